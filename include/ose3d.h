@@ -1,0 +1,205 @@
+/*
+ * ose3d.h - C ABI of libose3d.so, a single-GPU (sm_103a) one-step-extrapolation
+ * (OSE) acoustic modeler.
+ *
+ * The reference program (Littleke/3D-OSE) is one executable whose "interface"
+ * is its global parameter block (ose_3d.cu:42-63) and the host functions that
+ * main() calls around its time loop (ose_3d.cu:145-279).  Every entry point
+ * below replaces one group of those calls; the citation on each says which.
+ *
+ * Conventions
+ *   - Every function returns an ose_status (0 = OSE_OK).  Nothing throws across
+ *     the ABI and nothing calls exit().  ose_last_error() gives the message of
+ *     the last failure on a handle (or of ose_create when the handle is NULL).
+ *   - The library owns all device memory of a handle.  The caller owns every
+ *     host buffer; the library copies into and out of them.
+ *   - One host thread per handle at a time.  Several handles may coexist; each
+ *     runs on its own CUDA stream on the current device.
+ *   - Grids: nx, ny, nz are INTERIOR sizes.  Padded sizes are
+ *     nxb = bl + nx + br etc., with the trailing pad bumped by one when the
+ *     sum is odd (judge_odd, ose_3d_lib.cu:36-44).  Device fields are stored
+ *     [z][y][x] with x fastest (ose_3d.cu:226, plan dims (nzb, nyb, nxb)).
+ */
+#ifndef OSE3D_H
+#define OSE3D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ose_status {
+    OSE_OK = 0,
+    OSE_ERR_INVALID = 1,      /* bad argument or parameter */
+    OSE_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    OSE_ERR_NOMEM = 3,        /* device or host allocation failed */
+    OSE_ERR_IO = 4,           /* file could not be read or written */
+    OSE_ERR_UNSUPPORTED = 5,  /* size or mode outside what the kernels handle */
+    OSE_ERR_STATE = 6,        /* call out of order (e.g. ose_step before ose_reset_shot) */
+    OSE_ERR_NUMERIC = 7       /* non-finite value found in the wavefield */
+} ose_status;
+
+/* Sponge profile.  REFERENCE is generate_att (ose_3d_kernel.cu:242-261):
+ * exp(-((b-1-i)/b)^2) on the leading side, exp(-((i+1)/a)^2) on the trailing
+ * side, applied to the partial sum once per series term.  CERJAN is the
+ * classical exp(-(alpha*d)^2) taper, d = distance into the sponge in cells. */
+enum { OSE_SPONGE_REFERENCE = 0, OSE_SPONGE_CERJAN = 1 };
+
+/* Which field ose_get_wavefield / ose_set_wavefield address. */
+enum { OSE_FIELD_P = 0, OSE_FIELD_Q = 1, OSE_FIELD_V = 2 };
+
+/* Host layouts of a padded field. */
+enum {
+    OSE_LAYOUT_ZYX = 0,  /* [z][y][x], x fastest: the device layout          */
+    OSE_LAYOUT_YXZ = 1   /* [y][x][z], z fastest: write_3dfile_from_1darray_ci
+                            (ose_3d_lib.cu:364-380), the per-step wf dump */
+};
+
+/* Parameter block: the reference's hard-coded globals (ose_3d.cu:42-44,
+ * 75-118) plus a few switches whose zero value reproduces the reference. */
+typedef struct ose_params {
+    int nx, ny, nz;                 /* interior cells                        */
+    int bu, bd, bl, br, bf, bb;     /* sponge widths: up/down (z), left/right (x), front/back (y) */
+    int nt;                         /* time steps per shot                   */
+    float fm;                       /* Ricker peak frequency (Hz)            */
+    float dt;                       /* time step (s)                         */
+    float amp;                      /* Ricker amplitude                      */
+    float dx, dy, dz;               /* cell sizes (m)                        */
+    int nshot;                      /* shots (the reference runs 1)          */
+    int sxbeg, sybeg, szbeg;        /* first source, interior cell indices   */
+    int jsx, jsy, jsz;              /* source step between shots             */
+    int gxbeg, gybeg, gzbeg;        /* receiver origin; gzbeg = receiver depth */
+    int jgx, jgy, jgz;              /* receiver steps (kept for partest.txt)  */
+    int csdgather;                  /* kept for partest.txt                  */
+    /* switches; 0 = reference behaviour */
+    int sponge_mode;                /* OSE_SPONGE_*                          */
+    float cerjan_factor;            /* alpha for OSE_SPONGE_CERJAN (e.g. 0.015) */
+    int hilbert_div_nt;             /* 1: divide the Q source trace by nt.  The
+                                       reference does not (ose_3d_lib.cu:578-581),
+                                       so Q receives nt x the Hilbert transform. */
+    int M_override;                 /* >0: series order M; 0: (int)(dt*R) + 6
+                                       (ose_3d.cu:196-197)                   */
+} ose_params;
+
+/* Values derived from the parameters and the model (ose_3d.cu:85-90,120-122,
+ * 191-199), as used by the kernels. */
+typedef struct ose_derived {
+    int nxb, nyb, nzb;              /* padded sizes                          */
+    int br, bb, bd;                 /* trailing pads after the even-size fix */
+    int ng;                         /* receivers per shot = nx*ny            */
+    int M;                          /* series order: M+1 operator applications per step */
+    float vmax;                     /* max velocity of the padded model      */
+    double R;                       /* spectral radius bound vmax*pi*sqrt(1/dx^2+1/dy^2+1/dz^2) */
+    double dtR;                     /* dt*R                                  */
+    double dkx, dky, dkz;           /* 2*pi/(d*nb)                           */
+    double bessel_tail;             /* |J_{M+2}(dtR)|: first dropped series coefficient */
+    size_t device_bytes;            /* device memory held by the handle      */
+    int path;                       /* kernel family in use (OSE_PATH_*)     */
+} ose_derived;
+
+enum { OSE_PATH_GENERIC = 0, OSE_PATH_PLANE = 1 };
+
+typedef struct ose_handle ose_handle;
+
+/* Fill *p with the reference main()'s hard-coded values (ose_3d.cu:75-118). */
+ose_status ose_default_params(ose_params* p);
+
+/* Padded sizes of a parameter block (judge_odd, ose_3d_lib.cu:36-44). */
+ose_status ose_padded_dims(const ose_params* p, int* nxb, int* nyb, int* nzb);
+
+/* Create a handle: pad the interior model, build sponge, series and |k|
+ * tables, allocate and upload.  Replaces Alloc + input_file_xyz_boundary +
+ * add_pml_layers_v_h + data_R2CR + Alloc_mulGPU + find_max + R/M + the
+ * cufftXt plan/malloc/memcpy block (ose_3d.cu:145-237).
+ * vel_xyz: nx*ny*nz floats in the reference model layout [x][y][z], z fastest
+ * (input_file_xyz_boundary, ose_3d_lib.cu:887-909). */
+ose_status ose_create(const ose_params* p, const float* vel_xyz, ose_handle** out);
+
+/* Same, reading the raw float32 model file (ose_3d.cu:157-158). */
+ose_status ose_create_from_file(const ose_params* p, const char* path, ose_handle** out);
+
+/* Release every resource of the handle (Free_cufftXt + cufftDestroy + Free,
+ * ose_3d.cu:286-298).  NULL is accepted. */
+ose_status ose_destroy(ose_handle* h);
+
+/* Message of the last failure on h (or of the last failed ose_create when h
+ * is NULL).  The string stays valid until the next call on h. */
+const char* ose_last_error(const ose_handle* h);
+
+ose_status ose_get_derived(const ose_handle* h, ose_derived* d);
+
+/* Start shot `is`: zero P and Q, rebuild the shot's Ricker and Hilbert traces,
+ * clear the device gather and set it = 0.  Replaces Xtdata_value +
+ * Alloc_wavelet (ose_3d.cu:245-246, ose_3d_lib.cu:513-586). */
+ose_status ose_reset_shot(ose_handle* h, int is);
+
+/* One time step: inject the source sample of step it into P and Q,
+ * advance (P, Q) by dt with the OSE series, record Q on the receiver plane
+ * into the device gather row it, it += 1.  Replaces the body of the time loop
+ * (ose_3d.cu:252-274): Xt_add_wavelet_sxyz x2, wavefield_extro_ori2,
+ * rec_shotdata_3d and rec_slice_to_data. */
+ose_status ose_step(ose_handle* h);
+
+/* nsteps time steps as one replay of a captured CUDA graph (one step per
+ * graph node group; the step index lives in device memory).  gather_out may
+ * be NULL; otherwise it receives the WHOLE gather of the shot so far in the
+ * reference file order [ig][it] (ng x nt floats, write_3dfile_from_1darray
+ * with (ng,1,nt), ose_3d_lib.cu:327-343); rows of steps not run yet are 0. */
+ose_status ose_run(ose_handle* h, int nsteps, float* gather_out);
+
+/* As ose_run, but times the device work with CUDA events on the handle's
+ * stream and copies nothing back.  *ms receives the elapsed device time. */
+ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms);
+
+/* Steps taken in the current shot. */
+ose_status ose_get_it(const ose_handle* h, int* it);
+
+/* Copy a padded field to host (OSE_FIELD_P, _Q or _V) in the given layout.
+ * out holds nxb*nyb*nzb floats. */
+ose_status ose_get_wavefield(ose_handle* h, int which, float* out, int layout);
+
+/* Overwrite P or Q from a host buffer (padded, given layout). */
+ose_status ose_set_wavefield(ose_handle* h, int which, const float* in, int layout);
+
+/* Gather of the current shot in [ig][it] order (ng x nt floats). */
+ose_status ose_get_gather(ose_handle* h, float* out);
+
+/* The shot's source traces (nt floats each): the Ricker added to P and the
+ * Hilbert trace added to Q (generate_wavelet_gpu + hilbert_1d + C2R,
+ * ose_3d_lib.cu:575-583). */
+ose_status ose_get_wavelets(const ose_handle* h, float* ricker, float* hilbert);
+
+/* The 1-D sponge tables (nxb, nyb, nzb floats; generate_att). */
+ose_status ose_get_sponge(const ose_handle* h, float* ax, float* ay, float* az);
+
+/* Apply the normalised operator once to a packed complex field:
+ *   out = v * IFFT3(|k| * FFT3(in)) / (R * nxb*nyb*nzb)
+ * in/out are host arrays of nxb*nyb*nzb interleaved (re, im) float pairs,
+ * [z][y][x].  This is one application of the operator that
+ * wavefield_extro_ori2 applies 2(M+1) times per step (ose_3d_lib.cu:668-687:
+ * cufftXtExecDescriptorC2C forward, scale_kxkz_3D, inverse, scal_vr_3d); the
+ * real and imaginary parts carry two independent real fields. */
+ose_status ose_apply_operator(ose_handle* h, const float* in, float* out);
+
+/* Average device time per launch of each kernel class over one step, measured
+ * with CUDA events bracketing each launch on the handle's stream (not graph
+ * replay).  names/ms/bytes are arrays of capacity cap; *count receives the
+ * number of classes.  bytes = algorithmic HBM bytes of one launch. */
+ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count,
+                            const char** names, float* ms, double* bytes,
+                            int* launches_per_step);
+
+/* Write ./output-style files of the current shot:
+ * gather [ig][it] (ose_3d.cu:276) to gather_path and the parameter dump
+ * (output_par, ose_3d_lib.cu:255-319) to par_path.  Either may be NULL. */
+ose_status ose_write_outputs(ose_handle* h, const char* gather_path, const char* par_path);
+
+/* Library version string. */
+const char* ose_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OSE3D_H */
