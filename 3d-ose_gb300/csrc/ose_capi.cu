@@ -1,0 +1,655 @@
+// ose_capi.cu - the C ABI of libose3d.so (include/ose3d.h): handle lifetime,
+// device memory, the step sequence and its CUDA-graph replay.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "ose_internal.h"
+
+using ose::AxisPlan;
+
+struct ose_handle {
+    ose_params p{};
+    ose_derived d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    AxisPlan px{}, py{}, pz{};
+    ose::Geometry g{};
+    ose::Tables tables{};
+
+    // device memory (all owned)
+    float2* W = nullptr;     // state: P in .x, Q in .y  (a_0, and a_even during a step)
+    float2* A = nullptr;     // a_odd
+    float2* S = nullptr;     // partial sum
+    float2* X = nullptr;     // FFT scratch
+    float* vs = nullptr;     // v / (R N)
+    float *ax = nullptr, *ay = nullptr, *az = nullptr;
+    float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
+    float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
+    float *ricker = nullptr, *hil = nullptr;
+    float* gather = nullptr; // [nt][ng]
+    int* ctr = nullptr;      // [0] next step, [1] current step
+    size_t bytes = 0;
+
+    // host copies
+    std::vector<float> vb, h_ax, h_ay, h_az, h_ricker, h_hil;
+    std::vector<double> J;
+
+    long long src = 0;
+    int shot = -1;
+    int it = 0;
+    bool shot_ready = false;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ose::KernelTiming timing{};
+};
+
+namespace {
+
+std::string g_create_error;
+
+ose_status fail(ose_handle* h, ose_status s, const std::string& msg)
+{
+    if (h) h->err = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+ose_status cuda_fail(ose_handle* h, cudaError_t e, const char* what)
+{
+    return fail(h, OSE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, call)                                                          \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call);             \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(ose_handle* h, T** p, size_t count)
+{
+    size_t b = sizeof(T) * count;
+    cudaError_t e = cudaMalloc((void**)p, b);
+    if (e == cudaSuccess) h->bytes += b;
+    return e;
+}
+
+template <typename T>
+cudaError_t upload(ose_handle* h, T* dst, const std::vector<T>& src)
+{
+    return cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, h->stream);
+}
+
+void free_all(ose_handle* h)
+{
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    void* bufs[] = {h->W, h->A, h->S, h->X, h->vs, h->ax, h->ay, h->az, h->kx2, h->ky2, h->kz2,
+                    h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->timing.ev[0]) cudaEventDestroy(h->timing.ev[0]);
+    if (h->timing.ev[1]) cudaEventDestroy(h->timing.ev[1]);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+// Enqueue one whole time step on h->stream (no synchronisation).
+cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
+{
+    cudaError_t e;
+    if (tm) cudaEventRecord(tm->ev[0], h->stream);
+    e = ose::launch_inject(h->stream, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
+    if (tm) {
+        cudaEventRecord(tm->ev[1], h->stream);
+        cudaEventSynchronize(tm->ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[1]);
+        tm->ms[5] += ms;
+        tm->count[5] += 1;
+        tm->bytes[5] += 16.0;
+    }
+    if (e != cudaSuccess) return e;
+    const int M = h->d.M;
+    ose::EpiArgs ea{};
+    ea.vs = h->vs;
+    ea.ax = h->ax;
+    ea.ay = h->ay;
+    ea.az = h->az;
+    ea.S = h->S;
+    ea.wout = h->W;
+    ea.gather = h->gather;
+    ea.cur = h->ctr + 1;
+    ea.gz = h->p.bu + h->p.gzbeg;
+    ea.bl = h->p.bl;
+    ea.bf = h->p.bf;
+    ea.nx = h->p.nx;
+    ea.ny = h->p.ny;
+    ea.nt = h->p.nt;
+    const double N = (double)h->g.ncell;
+    // n = 0: a_1 = -i L a_0, S = J0 a_0 + 2 J1 a_1
+    ea.prev = h->A;
+    ea.w = h->W;
+    ea.c0 = (float)h->J[0];
+    ea.c1 = (float)(2.0 * h->J[1]);
+    e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->W, h->X,
+                                        ose::EPI_FIRST, ea, tm);
+    if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += 36.0 * N; }
+    if (e != cudaSuccess) return e;
+    for (int n = 1; n <= M; ++n) {
+        const float2* an = (n & 1) ? h->A : h->W;
+        ea.prev = (n & 1) ? h->W : h->A;
+        ea.c1 = (float)(2.0 * h->J[n + 1]);
+        e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, an, h->X,
+                                            n == M ? ose::EPI_LAST : ose::EPI_MID, ea, tm);
+        if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += (n == M ? 36.0 : 44.0) * N; }
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+ose_status build_graph(ose_handle* h)
+{
+    if (h->graph) return OSE_OK;
+    cudaGraph_t graph = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_step(h, nullptr);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(h, e, "capture step"); }
+    if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { h->graph = nullptr; return cuda_fail(h, e, "cudaGraphInstantiate"); }
+    return OSE_OK;
+}
+
+ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVALID; }
+
+void to_layout(const ose_handle* h, const float* zyx, float* out, int layout)
+{
+    const int nxb = h->d.nxb, nyb = h->d.nyb, nzb = h->d.nzb;
+    if (layout == OSE_LAYOUT_ZYX) {
+        memcpy(out, zyx, sizeof(float) * (size_t)nxb * nyb * nzb);
+        return;
+    }
+    size_t o = 0;   // [y][x][z] (write_3dfile_from_1darray_ci, ose_3d_lib.cu:374-377)
+    for (int y = 0; y < nyb; ++y)
+        for (int x = 0; x < nxb; ++x)
+            for (int z = 0; z < nzb; ++z) out[o++] = zyx[((size_t)z * nyb + y) * nxb + x];
+}
+
+void from_layout(const ose_handle* h, const float* in, float* zyx, int layout)
+{
+    const int nxb = h->d.nxb, nyb = h->d.nyb, nzb = h->d.nzb;
+    if (layout == OSE_LAYOUT_ZYX) {
+        memcpy(zyx, in, sizeof(float) * (size_t)nxb * nyb * nzb);
+        return;
+    }
+    size_t o = 0;
+    for (int y = 0; y < nyb; ++y)
+        for (int x = 0; x < nxb; ++x)
+            for (int z = 0; z < nzb; ++z) zyx[((size_t)z * nyb + y) * nxb + x] = in[o++];
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ose_version(void) { return "ose3d-gb300 0.1 (sm_103a)"; }
+
+ose_status ose_default_params(ose_params* p)
+{
+    if (!p) return OSE_ERR_INVALID;
+    memset(p, 0, sizeof(*p));
+    p->nx = p->ny = p->nz = 101;
+    p->bu = p->bd = p->bl = p->br = p->bf = p->bb = 25;
+    p->nt = 300;
+    p->fm = 40.0f;
+    p->dt = 0.001f;
+    p->amp = 100.0f;
+    p->dx = p->dy = p->dz = 10.0f;
+    p->nshot = 1;
+    p->sxbeg = p->nx / 2;
+    p->sybeg = p->ny / 2;
+    p->szbeg = 0;
+    p->jsx = p->jsy = p->jsz = 1;
+    p->jgx = p->jgy = p->jgz = 1;
+    return OSE_OK;
+}
+
+ose_status ose_padded_dims(const ose_params* p, int* nxb, int* nyb, int* nzb)
+{
+    if (!p || !nxb || !nyb || !nzb) return OSE_ERR_INVALID;
+    ose_derived d;
+    std::string err;
+    if (ose::derive_dims(*p, &d, &err)) return fail(nullptr, OSE_ERR_INVALID, err);
+    *nxb = d.nxb;
+    *nyb = d.nyb;
+    *nzb = d.nzb;
+    return OSE_OK;
+}
+
+const char* ose_last_error(const ose_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+ose_status ose_get_derived(const ose_handle* h, ose_derived* d)
+{
+    if (!h || !d) return OSE_ERR_INVALID;
+    *d = h->d;
+    d->device_bytes = h->bytes;
+    return OSE_OK;
+}
+
+ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
+{
+    if (!pin || !vel || !out) return fail(nullptr, OSE_ERR_INVALID, "null argument");
+    *out = nullptr;
+    ose_handle* h = new (std::nothrow) ose_handle();
+    if (!h) return fail(nullptr, OSE_ERR_NOMEM, "host allocation failed");
+    h->p = *pin;
+    std::string err;
+    if (ose::derive_dims(h->p, &h->d, &err)) { delete h; return fail(nullptr, OSE_ERR_INVALID, err); }
+    const ose_params& p = h->p;
+    ose_derived& d = h->d;
+    if (p.sponge_mode != OSE_SPONGE_REFERENCE && p.sponge_mode != OSE_SPONGE_CERJAN) {
+        delete h;
+        return fail(nullptr, OSE_ERR_INVALID, "unknown sponge_mode");
+    }
+    if (ose::plan_axis(d.nxb, &h->px) || ose::plan_axis(d.nyb, &h->py) || ose::plan_axis(d.nzb, &h->pz)) {
+        delete h;
+        return fail(nullptr, OSE_ERR_UNSUPPORTED, "padded axis longer than 1024 or not factorable");
+    }
+    if (p.gzbeg < 0 || p.gzbeg >= p.nz) {
+        delete h;
+        return fail(nullptr, OSE_ERR_INVALID, "receiver depth gzbeg outside the interior");
+    }
+    h->g.nxb = d.nxb;
+    h->g.nyb = d.nyb;
+    h->g.nzb = d.nzb;
+    h->g.ncell = (long long)d.nxb * d.nyb * d.nzb;
+    const size_t N = (size_t)h->g.ncell;
+
+    ose::pad_model(p, d, vel, h->vb);
+    float vmax = -9999999.999f;    // find_max (ose_3d_lib.cu:544-555)
+    for (float v : h->vb) vmax = v > vmax ? v : vmax;
+    if (!(vmax > 0.f) || !std::isfinite(vmax)) { delete h; return fail(nullptr, OSE_ERR_INVALID, "velocity model must be positive and finite"); }
+    for (float v : h->vb)
+        if (!(v > 0.f) || !std::isfinite(v)) { delete h; return fail(nullptr, OSE_ERR_INVALID, "velocity model must be positive and finite"); }
+    ose::series_params(p, vmax, &d);
+    h->J.resize(d.M + 2);
+    for (int n = 0; n <= d.M + 1; ++n) h->J[n] = jn(n, d.dtR);
+    ose::sponge_table(p.bl, p.nx, d.br, p.sponge_mode, p.cerjan_factor, h->h_ax);
+    ose::sponge_table(p.bf, p.ny, d.bb, p.sponge_mode, p.cerjan_factor, h->h_ay);
+    ose::sponge_table(p.bu, p.nz, d.bd, p.sponge_mode, p.cerjan_factor, h->h_az);
+    std::vector<float> kx2, ky2, kz2, vs(N);
+    ose::k2_table(d.nxb, d.dkx, kx2);
+    ose::k2_table(d.nyb, d.dky, ky2);
+    ose::k2_table(d.nzb, d.dkz, kz2);
+    std::vector<float2> twx, twy, twz;
+    ose::twiddle_table(d.nxb, twx);
+    ose::twiddle_table(d.nyb, twy);
+    ose::twiddle_table(d.nzb, twz);
+    const double sc = 1.0 / (d.R * (double)N);
+    for (size_t i = 0; i < N; ++i) vs[i] = (float)((double)h->vb[i] * sc);
+
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { ose_status s = cuda_fail(nullptr, e, "cudaGetDevice"); delete h; return s; }
+#define CKC(call)                                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ose_status s_ = cuda_fail(nullptr, e_, #call);                          \
+            if (e_ == cudaErrorMemoryAllocation) s_ = OSE_ERR_NOMEM;                \
+            free_all(h);                                                            \
+            delete h;                                                               \
+            return s_;                                                              \
+        }                                                                           \
+    } while (0)
+    CKC(ose::configure_kernels());
+    CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CKC(cudaEventCreate(&h->ev0));
+    CKC(cudaEventCreate(&h->ev1));
+    CKC(cudaEventCreate(&h->timing.ev[0]));
+    CKC(cudaEventCreate(&h->timing.ev[1]));
+    CKC(dalloc(h, &h->W, N));
+    CKC(dalloc(h, &h->A, N));
+    CKC(dalloc(h, &h->S, N));
+    CKC(dalloc(h, &h->X, N));
+    CKC(dalloc(h, &h->vs, N));
+    CKC(dalloc(h, &h->ax, d.nxb));
+    CKC(dalloc(h, &h->ay, d.nyb));
+    CKC(dalloc(h, &h->az, d.nzb));
+    CKC(dalloc(h, &h->kx2, d.nxb));
+    CKC(dalloc(h, &h->ky2, d.nyb));
+    CKC(dalloc(h, &h->kz2, d.nzb));
+    CKC(dalloc(h, &h->twx, d.nxb));
+    CKC(dalloc(h, &h->twy, d.nyb));
+    CKC(dalloc(h, &h->twz, d.nzb));
+    CKC(dalloc(h, &h->ricker, (size_t)p.nt));
+    CKC(dalloc(h, &h->hil, (size_t)p.nt));
+    CKC(dalloc(h, &h->gather, (size_t)p.nt * d.ng));
+    CKC(dalloc(h, &h->ctr, 4));
+    CKC(upload(h, h->vs, vs));
+    CKC(upload(h, h->ax, h->h_ax));
+    CKC(upload(h, h->ay, h->h_ay));
+    CKC(upload(h, h->az, h->h_az));
+    CKC(upload(h, h->kx2, kx2));
+    CKC(upload(h, h->ky2, ky2));
+    CKC(upload(h, h->kz2, kz2));
+    CKC(upload(h, h->twx, twx));
+    CKC(upload(h, h->twy, twy));
+    CKC(upload(h, h->twz, twz));
+    CKC(cudaMemsetAsync(h->W, 0, sizeof(float2) * N, h->stream));
+    CKC(cudaMemsetAsync(h->ctr, 0, sizeof(int) * 4, h->stream));
+    CKC(cudaStreamSynchronize(h->stream));
+#undef CKC
+    h->tables.twx = h->twx;
+    h->tables.twy = h->twy;
+    h->tables.twz = h->twz;
+    h->tables.kx2 = h->kx2;
+    h->tables.ky2 = h->ky2;
+    h->tables.kz2 = h->kz2;
+    d.path = OSE_PATH_GENERIC;
+    d.device_bytes = h->bytes;
+    *out = h;
+    return OSE_OK;
+}
+
+ose_status ose_create_from_file(const ose_params* p, const char* path, ose_handle** out)
+{
+    if (!p || !path || !out) return fail(nullptr, OSE_ERR_INVALID, "null argument");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(nullptr, OSE_ERR_IO, std::string("cannot open ") + path);
+    const size_t n = (size_t)p->nx * p->ny * p->nz;
+    std::vector<float> v(n);
+    size_t got = fread(v.data(), sizeof(float), n, f);
+    fclose(f);
+    if (got != n) return fail(nullptr, OSE_ERR_IO, std::string("short model file ") + path);
+    return ose_create(p, v.data(), out);
+}
+
+ose_status ose_destroy(ose_handle* h)
+{
+    if (!h) return OSE_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return OSE_OK;
+}
+
+ose_status ose_reset_shot(ose_handle* h, int is)
+{
+    if (!h) return OSE_ERR_INVALID;
+    const ose_params& p = h->p;
+    if (is < 0) return fail(h, OSE_ERR_INVALID, "negative shot index");
+    // source: sg_init_host then the decode of Xt_add_wavelet_sxyz (ose_3d_lib.cu:598-616)
+    const long long nxy = (long long)p.nx * p.ny;
+    const long long sx0 = p.sxbeg + (long long)is * p.jsx, sy0 = p.sybeg + (long long)is * p.jsy,
+                    sz0 = p.szbeg + (long long)is * p.jsz;
+    const long long sxyz = sz0 * nxy + sy0 * p.nx + sx0;
+    if (sxyz < 0) return fail(h, OSE_ERR_INVALID, "source outside the model");
+    const long long sx = sxyz % nxy % p.nx, sy = sxyz % nxy / p.nx, sz = sxyz / nxy;
+    const long long X = p.bl + sx, Y = p.bf + sy, Z = p.bu + sz;
+    if (X >= h->d.nxb || Y >= h->d.nyb || Z >= h->d.nzb)
+        return fail(h, OSE_ERR_INVALID, "source outside the padded grid");
+    h->src = (Z * h->d.nyb + Y) * h->d.nxb + X;
+    // Alloc_wavelet (ose_3d_lib.cu:557-586)
+    ose::ricker_trace(p.nt, p.fm, p.dt, p.amp, h->h_ricker);
+    ose::hilbert_trace(h->h_ricker, p.hilbert_div_nt, h->h_hil);
+    const size_t N = (size_t)h->g.ncell;
+    CK(h, upload(h, h->ricker, h->h_ricker));
+    CK(h, upload(h, h->hil, h->h_hil));
+    // Xtdata_value: the state starts at rest
+    CK(h, cudaMemsetAsync(h->W, 0, sizeof(float2) * N, h->stream));
+    CK(h, cudaMemsetAsync(h->gather, 0, sizeof(float) * (size_t)p.nt * h->d.ng, h->stream));
+    CK(h, cudaMemsetAsync(h->ctr, 0, sizeof(int) * 4, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }   // src may have moved
+    h->shot = is;
+    h->it = 0;
+    h->shot_ready = true;
+    return OSE_OK;
+}
+
+ose_status ose_step(ose_handle* h)
+{
+    if (!h) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    if (h->it >= h->p.nt) return fail(h, OSE_ERR_STATE, "all nt steps of the shot are done");
+    CK(h, enqueue_step(h, nullptr));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->it += 1;
+    return OSE_OK;
+}
+
+static ose_status run_graph(ose_handle* h, int nsteps)
+{
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    if (nsteps < 0 || h->it + nsteps > h->p.nt) return fail(h, OSE_ERR_INVALID, "nsteps beyond nt");
+    ose_status s = build_graph(h);
+    if (s != OSE_OK) return s;
+    for (int i = 0; i < nsteps; ++i) CK(h, cudaGraphLaunch(h->graph, h->stream));
+    return OSE_OK;
+}
+
+ose_status ose_run(ose_handle* h, int nsteps, float* gather_out)
+{
+    if (!h) return OSE_ERR_INVALID;
+    ose_status s = run_graph(h, nsteps);
+    if (s != OSE_OK) return s;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->it += nsteps;
+    if (gather_out) return ose_get_gather(h, gather_out);
+    return OSE_OK;
+}
+
+ose_status ose_run_record(ose_handle* h, int nsteps, float* rows_out)
+{
+    if (!h || !rows_out) return OSE_ERR_INVALID;
+    const int ng = h->d.ng;
+    for (int i = 0; i < nsteps; ++i) {
+        const int it = h->it;
+        ose_status s = run_graph(h, 1);
+        if (s != OSE_OK) return s;
+        CK(h, cudaMemcpyAsync(rows_out + (size_t)i * ng, h->gather + (size_t)it * ng, sizeof(float) * ng,
+                              cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        h->it += 1;
+    }
+    return OSE_OK;
+}
+
+ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms)
+{
+    if (!h || !ms) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    ose_status s = build_graph(h);
+    if (s != OSE_OK) return s;
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaEventRecord(h->ev0, h->stream));
+    s = run_graph(h, nsteps);
+    if (s != OSE_OK) return s;
+    CK(h, cudaEventRecord(h->ev1, h->stream));
+    CK(h, cudaEventSynchronize(h->ev1));
+    CK(h, cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    h->it += nsteps;
+    return OSE_OK;
+}
+
+ose_status ose_get_it(const ose_handle* h, int* it)
+{
+    if (!h || !it) return OSE_ERR_INVALID;
+    *it = h->it;
+    return OSE_OK;
+}
+
+ose_status ose_get_gather(ose_handle* h, float* out)
+{
+    if (!h || !out) return OSE_ERR_INVALID;
+    const int nt = h->p.nt, ng = h->d.ng;
+    std::vector<float> g((size_t)nt * ng);
+    CK(h, cudaMemcpyAsync(g.data(), h->gather, sizeof(float) * g.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int it = 0; it < nt; ++it)        // [it][ig] -> [ig][it] (ose_3d_lib.cu:327-343)
+        for (int ig = 0; ig < ng; ++ig) out[(size_t)ig * nt + it] = g[(size_t)it * ng + ig];
+    return OSE_OK;
+}
+
+ose_status ose_get_wavefield(ose_handle* h, int which, float* out, int layout)
+{
+    if (!h || !out) return OSE_ERR_INVALID;
+    if (layout != OSE_LAYOUT_ZYX && layout != OSE_LAYOUT_YXZ) return fail(h, OSE_ERR_INVALID, "bad layout");
+    const size_t N = (size_t)h->g.ncell;
+    std::vector<float> zyx(N);
+    if (which == OSE_FIELD_V) {
+        zyx = h->vb;
+    } else if (which == OSE_FIELD_P || which == OSE_FIELD_Q) {
+        std::vector<float2> w(N);
+        CK(h, cudaMemcpyAsync(w.data(), h->W, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        for (size_t i = 0; i < N; ++i) zyx[i] = which == OSE_FIELD_P ? w[i].x : w[i].y;
+    } else {
+        return fail(h, OSE_ERR_INVALID, "bad field");
+    }
+    to_layout(h, zyx.data(), out, layout);
+    return OSE_OK;
+}
+
+ose_status ose_set_wavefield(ose_handle* h, int which, const float* in, int layout)
+{
+    if (!h || !in) return OSE_ERR_INVALID;
+    if (which != OSE_FIELD_P && which != OSE_FIELD_Q) return fail(h, OSE_ERR_INVALID, "only P or Q can be set");
+    if (layout != OSE_LAYOUT_ZYX && layout != OSE_LAYOUT_YXZ) return fail(h, OSE_ERR_INVALID, "bad layout");
+    const size_t N = (size_t)h->g.ncell;
+    std::vector<float> zyx(N);
+    from_layout(h, in, zyx.data(), layout);
+    std::vector<float2> w(N);
+    CK(h, cudaMemcpyAsync(w.data(), h->W, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < N; ++i) (which == OSE_FIELD_P ? w[i].x : w[i].y) = zyx[i];
+    CK(h, cudaMemcpyAsync(h->W, w.data(), sizeof(float2) * N, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return OSE_OK;
+}
+
+ose_status ose_get_wavelets(const ose_handle* h, float* ricker, float* hilbert)
+{
+    if (!h) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return OSE_ERR_STATE;
+    if (ricker) memcpy(ricker, h->h_ricker.data(), sizeof(float) * h->p.nt);
+    if (hilbert) memcpy(hilbert, h->h_hil.data(), sizeof(float) * h->p.nt);
+    return OSE_OK;
+}
+
+ose_status ose_get_sponge(const ose_handle* h, float* ax, float* ay, float* az)
+{
+    if (!h) return OSE_ERR_INVALID;
+    if (ax) memcpy(ax, h->h_ax.data(), sizeof(float) * h->h_ax.size());
+    if (ay) memcpy(ay, h->h_ay.data(), sizeof(float) * h->h_ay.size());
+    if (az) memcpy(az, h->h_az.data(), sizeof(float) * h->h_az.size());
+    return OSE_OK;
+}
+
+ose_status ose_apply_operator(ose_handle* h, const float* in, float* out)
+{
+    if (!h || !in || !out) return OSE_ERR_INVALID;
+    const size_t N = (size_t)h->g.ncell;
+    // A and S carry no state between steps, so they serve as in/out here.
+    CK(h, cudaMemcpyAsync(h->A, in, sizeof(float2) * N, cudaMemcpyHostToDevice, h->stream));
+    CK(h, ose::launch_apply_operator(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->A, h->X, h->S, h->vs));
+    CK(h, cudaMemcpyAsync(out, h->S, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return OSE_OK;
+}
+
+ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const char** names,
+                            float* ms, double* bytes, int* launches_per_step)
+{
+    if (!h || !count || reps < 1) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    if (h->it + reps > h->p.nt) return fail(h, OSE_ERR_INVALID, "reps beyond nt");
+    ose::KernelTiming& t = h->timing;
+    static const char* kNames[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
+                                   "fft_x_inv_epilogue", "inject"};
+    const int nc = 6;
+    for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
+    for (int r = 0; r < reps; ++r) {
+        CK(h, enqueue_step(h, &t));
+        CK(h, cudaStreamSynchronize(h->stream));
+        h->it += 1;
+    }
+    *count = nc;
+    int total = 0;
+    for (int c = 0; c < nc && c < cap; ++c) {
+        if (names) names[c] = kNames[c];
+        if (ms) ms[c] = t.count[c] ? t.ms[c] / t.count[c] : 0.f;
+        if (bytes) bytes[c] = t.count[c] ? t.bytes[c] / t.count[c] : 0.0;
+        total += t.count[c];
+    }
+    if (launches_per_step) *launches_per_step = total / reps;
+    return OSE_OK;
+}
+
+ose_status ose_write_outputs(ose_handle* h, const char* gather_path, const char* par_path)
+{
+    if (!h) return OSE_ERR_INVALID;
+    const ose_params& p = h->p;
+    if (gather_path) {
+        std::vector<float> g((size_t)p.nt * h->d.ng);
+        ose_status s = ose_get_gather(h, g.data());
+        if (s != OSE_OK) return s;
+        FILE* f = fopen(gather_path, "wb");
+        if (!f) return fail(h, OSE_ERR_IO, std::string("cannot write ") + gather_path);
+        size_t w = fwrite(g.data(), sizeof(float), g.size(), f);
+        fclose(f);
+        if (w != g.size()) return fail(h, OSE_ERR_IO, std::string("short write ") + gather_path);
+    }
+    if (par_path) {
+        // output_par (ose_3d_lib.cu:255-319): label line, value line, same labels
+        FILE* f = fopen(par_path, "wb");
+        if (!f) return fail(h, OSE_ERR_IO, std::string("cannot write ") + par_path);
+        struct { const char* label; int iv; float fv; bool is_f; } rows[] = {
+            {"X dimension size----> nx\n", p.nx, 0, false},
+            {"Y dimension size----> ny\n", p.ny, 0, false},
+            {"Z dimension size----> ny\n", p.nz, 0, false},
+            {"The interval of samples in space domain X dimension ----> dx (the units is 'mile')\n", 0, p.dx, true},
+            {"The interval of samples in space domain Y dimension ----> dy (the units is 'mile')\n", 0, p.dy, true},
+            {"The interval of samples in space domain Z dimension ----> dz (the units is 'mile')\n", 0, p.dz, true},
+            {"The number of samples in time domain ----> nt\n", p.nt, 0, false},
+            {"The number of receivers gather ----> ng\n", h->d.ng, 0, false},
+            {"The number of sources ----> ns\n", p.nshot, 0, false},
+            {"The interval of samples in time domain (the units is 's') ----> dt\n", 0, p.dt, true},
+            {"The amplitude of wavelet ----> amp\n", 0, p.amp, true},
+            {"The main frequency of wavelet ----> fm\n", 0, p.fm, true},
+            {"The beginning location of sources in X-axis ----> sxbeg\n", p.sxbeg, 0, false},
+            {"The beginning location of sources in Y-axis ----> sxbeg\n", p.sybeg, 0, false},
+            {"The beginning location of sources in Z-axis ----> szbeg\n", p.szbeg, 0, false},
+            {"The beginning location of receivers in X-axis ----> gxbeg\n", p.gxbeg, 0, false},
+            {"The beginning location of receivers in Y-axis ----> gybeg\n", p.gybeg, 0, false},
+            {"The beginning location of receivers in Z-axis ----> gzbeg\n", p.gzbeg, 0, false},
+            {"Sources X-axis  jump interval ----> jsx\n", p.jsx, 0, false},
+            {"Sources Y-axis  jump interval ----> jsy\n", p.jsy, 0, false},
+            {"Sources Z-axis  jump interval ----> jsz\n", p.jsz, 0, false},
+            {"Receivers X-axis  jump interval ----> jgx\n", p.jgx, 0, false},
+            {"Receivers Y-axis  jump interval ----> jgy\n", p.jgy, 0, false},
+            {"Receivers Z-axis  jump interval ----> jgzn", p.jgz, 0, false},
+            {"Default, common shot-gather; if n, record at every point\n", p.csdgather, 0, false},
+        };
+        for (auto& r : rows) {
+            fputs(r.label, f);
+            if (r.is_f) fprintf(f, "%f\n", r.fv);
+            else fprintf(f, "%d\n", r.iv);
+        }
+        fclose(f);
+    }
+    return OSE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,410 @@
+// ose_kernels.cu - generic-size kernels of one OSE operator application
+// (any even padded size, axes up to 1024 with radices 4, 2, 3, 5, 7 and a
+// direct DFT for other primes).
+//
+// One application of L = v * IFFT3(|k| FFT3(.)) / (R N) to the packed field
+// a_n = p + i q (wavefield_extro_ori2, ose_3d_lib.cu:665-687 for one part) is
+// five passes over HBM:
+//   1. x rows   forward   a_n -> X
+//   2. y lines  forward   X in place
+//   3. z lines  forward, * |k|, inverse   X in place (scale_kxkz_3D fused
+//      between the two z transforms)
+//   4. y lines  inverse   X in place
+//   5. x rows   inverse + the step's pointwise work: v/(R N) (scal_vr_3d),
+//      recurrence a_{n+1} = a_{n-1} - 2i L a_n, S += 2 J_{n+1} a_{n+1}
+//      (add_bessel_3d), S *= sponge (apply_ABC_Xt), and on the last term the
+//      new state and the receiver row (rec_shotdata_3d).
+// Each pass stages a tile of lines in shared memory and runs a Stockham
+// autosort FFT there (natural order in, natural order out).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ose_internal.h"
+
+namespace ose {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+template <bool INV>
+__device__ __forceinline__ float2 twiddle(const float2* tw, int e)
+{
+    float2 w = tw[e];
+    return INV ? make_float2(w.x, -w.y) : w;
+}
+
+// times W_4 = -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 rot4(float2 a)
+{
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// One Stockham stage of radix r on L lines: element e of line l sits at
+// buf[l*LS + e*ES].  p = product of the radices already applied.
+template <bool INV>
+__device__ void fft_stage(const float2* __restrict__ in, float2* __restrict__ out, int L, int LS,
+                          int ES, bool line_fastest, int n, int r, int p, const float2* tw)
+{
+    const int m = n / r;
+    const int tstep = n / (p * r);
+    const int total = L * m;
+    for (int b = threadIdx.x; b < total; b += blockDim.x) {
+        int l, i;
+        if (line_fastest) { l = b % L; i = b / L; }
+        else { l = b / m; i = b - l * m; }
+        const int k = i % p;
+        const int te = k * tstep;
+        const float2* src = in + l * LS + i * ES;
+        float2* dst = out + l * LS + ((i - k) * r + k) * ES;
+        const int ms = m * ES, ps = p * ES;
+        if (r == 4) {
+            float2 x0 = src[0], x1 = src[ms], x2 = src[2 * ms], x3 = src[3 * ms];
+            if (te) {
+                x1 = cmul(x1, twiddle<INV>(tw, te));
+                x2 = cmul(x2, twiddle<INV>(tw, 2 * te));
+                x3 = cmul(x3, twiddle<INV>(tw, 3 * te));
+            }
+            float2 a0 = cadd(x0, x2), a1 = csub(x0, x2), a2 = cadd(x1, x3), a3 = rot4<INV>(csub(x1, x3));
+            dst[0] = cadd(a0, a2);
+            dst[ps] = cadd(a1, a3);
+            dst[2 * ps] = csub(a0, a2);
+            dst[3 * ps] = csub(a1, a3);
+        } else if (r == 2) {
+            float2 x0 = src[0], x1 = src[ms];
+            if (te) x1 = cmul(x1, twiddle<INV>(tw, te));
+            dst[0] = cadd(x0, x1);
+            dst[ps] = csub(x0, x1);
+        } else if (r == 3) {
+            float2 x0 = src[0], x1 = src[ms], x2 = src[2 * ms];
+            if (te) {
+                x1 = cmul(x1, twiddle<INV>(tw, te));
+                x2 = cmul(x2, twiddle<INV>(tw, 2 * te));
+            }
+            const float h = 0.866025403784438647f;   // sqrt(3)/2
+            float2 s = cadd(x1, x2), d = csub(x1, x2);
+            float2 t = make_float2(x0.x - 0.5f * s.x, x0.y - 0.5f * s.y);
+            // forward: y1 = t - i h d, y2 = t + i h d
+            float2 ihd = INV ? make_float2(-h * d.y, h * d.x) : make_float2(h * d.y, -h * d.x);
+            dst[0] = cadd(x0, s);
+            dst[ps] = cadd(t, ihd);
+            dst[2 * ps] = csub(t, ihd);
+        } else {
+            const int nr = n / r;
+            for (int q = 0; q < r; ++q) {
+                float2 acc = make_float2(0.f, 0.f);
+                for (int j = 0; j < r; ++j) {
+                    float2 x = src[j * ms];
+                    if (te) x = cmul(x, twiddle<INV>(tw, j * te));
+                    acc = cadd(acc, cmul(x, twiddle<INV>(tw, ((j * q) % r) * nr)));
+                }
+                dst[q * ps] = acc;
+            }
+        }
+    }
+}
+
+// Full transform of L lines held in a; returns the buffer holding the result.
+template <bool INV>
+__device__ float2* fft_lines(float2* a, float2* b, int L, int LS, int ES, bool line_fastest,
+                             const AxisPlan& pl, const float2* tw)
+{
+    int p = 1;
+    for (int s = 0; s < pl.ns; ++s) {
+        const int r = pl.radix[s];
+        fft_stage<INV>(a, b, L, LS, ES, line_fastest, pl.n, r, p, tw);
+        __syncthreads();
+        p *= r;
+        float2* t = a; a = b; b = t;
+    }
+    return a;
+}
+
+enum { EPI_NONE = -1, EPI_SCALE = 3 };
+
+// The pointwise work of one application on cell i = (x, y, z); X is the
+// unnormalised inverse transform.
+template <int EPI>
+__device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float2 X, const EpiArgs& e)
+{
+    const float v = __ldg(e.vs + i);
+    const float2 Lx = cscale(X, v);
+    if (EPI == EPI_SCALE) {
+        e.prev[i] = Lx;
+    } else if (EPI == EPI_FIRST) {
+        // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1   (ose_3d_lib.cu:651-744)
+        const float2 a1 = make_float2(Lx.y, -Lx.x);
+        const float2 w = e.w[i];
+        e.prev[i] = a1;
+        e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+    } else {
+        // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
+        const float2 am = e.prev[i];
+        const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
+        const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
+        float2 s = e.S[i];
+        s.x = fmaf(e.c1, an.x, s.x) * att;
+        s.y = fmaf(e.c1, an.y, s.y) * att;
+        if (EPI == EPI_MID) {
+            e.prev[i] = an;
+            e.S[i] = s;
+        } else {
+            e.wout[i] = s;
+            if (z == e.gz) {
+                const int ix = x - e.bl, iy = y - e.bf;
+                if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
+                    const int c = *e.cur;
+                    if (c >= 0 && c < e.nt) e.gather[(long long)c * e.nx * e.ny + iy * e.nx + ix] = s.y;
+                }
+            }
+        }
+    }
+}
+
+// Pass over x rows: rows_per_cta consecutive rows (one contiguous block).
+template <bool INV, int EPI>
+__global__ void __launch_bounds__(kThreads) k_rows(const float2* __restrict__ src, float2* __restrict__ dst,
+                                                   Geometry g, AxisPlan pl, const float2* __restrict__ twg,
+                                                   int rows_per_cta, EpiArgs e)
+{
+    extern __shared__ float4 smem4[];
+    float2* sm = reinterpret_cast<float2*>(smem4);
+    const int n = pl.n;
+    const long long nrows = (long long)g.nyb * g.nzb;
+    const long long row0 = (long long)blockIdx.x * rows_per_cta;
+    const int rows = (int)min((long long)rows_per_cta, nrows - row0);
+    float2* tw = sm;
+    float2* A = sm + n;
+    float2* B = A + (size_t)rows_per_cta * n;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
+    const int nv = rows * n / 2;   // float4 = two complex values; n is even
+    const float4* s4 = reinterpret_cast<const float4*>(src + row0 * n);
+    float4* A4 = reinterpret_cast<float4*>(A);
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) A4[t] = s4[t];
+    __syncthreads();
+    float2* R = fft_lines<INV>(A, B, rows, n, 1, false, pl, tw);
+    if (EPI == EPI_NONE) {
+        float4* d4 = reinterpret_cast<float4*>(dst + row0 * n);
+        const float4* R4 = reinterpret_cast<const float4*>(R);
+        for (int t = threadIdx.x; t < nv; t += blockDim.x) d4[t] = R4[t];
+    } else {
+        for (int t = threadIdx.x; t < rows * n; t += blockDim.x) {
+            const int r = t / n, x = t - r * n;
+            const long long row = row0 + r;
+            const int y = (int)(row % g.nyb), z = (int)(row / g.nyb);
+            epilogue<EPI>(row0 * n + t, x, y, z, R[t], e);
+        }
+    }
+}
+
+// Pass over lines of stride `stride` (y: nxb, z: nxb*nyb); a CTA takes TX
+// neighbouring x columns so every global access is a TX-wide row segment.
+// KSCALE: forward, * |k|, inverse (the z pass).
+template <bool INV, bool KSCALE>
+__global__ void __launch_bounds__(kThreads) k_lines(float2* __restrict__ data, Geometry g, AxisPlan pl,
+                                                    const float2* __restrict__ twg, int TX,
+                                                    long long stride, Tables tb)
+{
+    extern __shared__ float4 smem4[];
+    float2* sm = reinterpret_cast<float2*>(smem4);
+    const int n = pl.n;
+    float2* tw = sm;
+    float2* A = sm + n;
+    float2* B = A + (size_t)n * TX;
+    const int x0 = blockIdx.x * TX;
+    const int cols = min(TX, g.nxb - x0);
+    // blockIdx.y: the other index (z for the y pass, y for the z pass)
+    const long long base = KSCALE ? (long long)blockIdx.y * g.nxb + x0
+                                  : (long long)blockIdx.y * g.nyb * g.nxb + x0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
+    for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+        const int e = t / TX, c = t - e * TX;
+        A[t] = c < cols ? data[base + e * stride + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2* R;
+    if (KSCALE) {
+        R = fft_lines<false>(A, B, TX, 1, TX, true, pl, tw);
+        float2* O = R == A ? B : A;
+        const float ky2 = tb.ky2[blockIdx.y];
+        for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+            const int z = t / TX, c = t - z * TX;
+            const float kx2 = c < cols ? tb.kx2[x0 + c] : 0.f;
+            R[t] = cscale(R[t], sqrtf(kx2 + ky2 + tb.kz2[z]));
+        }
+        __syncthreads();
+        R = fft_lines<true>(R, O, TX, 1, TX, true, pl, tw);
+    } else {
+        R = fft_lines<INV>(A, B, TX, 1, TX, true, pl, tw);
+    }
+    for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+        const int e = t / TX, c = t - e * TX;
+        if (c < cols) data[base + e * stride + c] = R[t];
+    }
+}
+
+int rows_per_cta(int n) { return n >= 2048 ? 1 : 2048 / n; }
+int tile_x(int n) { return n <= 640 ? 16 : 8; }
+size_t rows_smem(int n) { return sizeof(float2) * ((size_t)n + 2 * (size_t)rows_per_cta(n) * n); }
+size_t lines_smem(int n) { return sizeof(float2) * ((size_t)n + 2 * (size_t)n * tile_x(n)); }
+
+template <typename K>
+cudaError_t allow_smem(K k)
+{
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+struct Timer {
+    KernelTiming* t;
+    cudaStream_t s;
+    int cls;
+    Timer(KernelTiming* tt, cudaStream_t ss, int c) : t(tt), s(ss), cls(c)
+    {
+        if (t) cudaEventRecord(t->ev[0], s);
+    }
+    void done()
+    {
+        if (!t) return;
+        cudaEventRecord(t->ev[1], s);
+        cudaEventSynchronize(t->ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]);
+        t->ms[cls] += ms;
+        t->count[cls] += 1;
+    }
+};
+
+}  // namespace
+
+cudaError_t configure_kernels()
+{
+    cudaError_t e;
+#define ALLOW(k) if ((e = allow_smem(k)) != cudaSuccess) return e
+    ALLOW((k_rows<false, EPI_NONE>));
+    ALLOW((k_rows<true, EPI_FIRST>));
+    ALLOW((k_rows<true, EPI_MID>));
+    ALLOW((k_rows<true, EPI_LAST>));
+    ALLOW((k_rows<true, EPI_SCALE>));
+    ALLOW((k_lines<false, false>));
+    ALLOW((k_lines<true, false>));
+    ALLOW((k_lines<false, true>));
+#undef ALLOW
+    return cudaSuccess;
+}
+
+// Timing classes of the generic path.
+enum { T_XF = 0, T_YF = 1, T_ZK = 2, T_YI = 3, T_XI = 4, T_INJ = 5 };
+
+static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPlan& px,
+                                 const AxisPlan& py, const AxisPlan& pz, const Tables& t,
+                                 const float2* an, float2* X, KernelTiming* tm)
+{
+    EpiArgs none{};
+    const long long nrows = (long long)g.nyb * g.nzb;
+    {
+        Timer T(tm, s, T_XF);
+        const int rpc = rows_per_cta(px.n);
+        k_rows<false, EPI_NONE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
+            an, X, g, px, t.twx, rpc, none);
+        T.done();
+    }
+    {
+        Timer T(tm, s, T_YF);
+        const int tx = tile_x(py.n);
+        dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
+        k_lines<false, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        T.done();
+    }
+    {
+        Timer T(tm, s, T_ZK);
+        const int tx = tile_x(pz.n);
+        dim3 grid((g.nxb + tx - 1) / tx, g.nyb);
+        k_lines<false, true><<<grid, kThreads, lines_smem(pz.n), s>>>(X, g, pz, t.twz, tx,
+                                                                     (long long)g.nxb * g.nyb, t);
+        T.done();
+    }
+    {
+        Timer T(tm, s, T_YI);
+        const int tx = tile_x(py.n);
+        dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
+        k_lines<true, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        T.done();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const AxisPlan& px,
+                                       const AxisPlan& py, const AxisPlan& pz, const Tables& t,
+                                       const float2* an, float2* X, EpiMode mode, const EpiArgs& e,
+                                       KernelTiming* tm)
+{
+    cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, an, X, tm);
+    if (err != cudaSuccess) return err;
+    const long long nrows = (long long)g.nyb * g.nzb;
+    const int rpc = rows_per_cta(px.n);
+    const unsigned nb = (unsigned)((nrows + rpc - 1) / rpc);
+    Timer T(tm, s, T_XI);
+    switch (mode) {
+    case EPI_FIRST:
+        k_rows<true, EPI_FIRST><<<nb, kThreads, rows_smem(px.n), s>>>(X, nullptr, g, px, t.twx, rpc, e);
+        break;
+    case EPI_MID:
+        k_rows<true, EPI_MID><<<nb, kThreads, rows_smem(px.n), s>>>(X, nullptr, g, px, t.twx, rpc, e);
+        break;
+    default:
+        k_rows<true, EPI_LAST><<<nb, kThreads, rows_smem(px.n), s>>>(X, nullptr, g, px, t.twx, rpc, e);
+        break;
+    }
+    T.done();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisPlan& px,
+                                  const AxisPlan& py, const AxisPlan& pz, const Tables& t,
+                                  const float2* in, float2* X, float2* out, const float* vs)
+{
+    cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, in, X, nullptr);
+    if (err != cudaSuccess) return err;
+    EpiArgs e{};
+    e.prev = out;
+    e.vs = vs;
+    const long long nrows = (long long)g.nyb * g.nzb;
+    const int rpc = rows_per_cta(px.n);
+    k_rows<true, EPI_SCALE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
+        X, nullptr, g, px, t.twx, rpc, e);
+    return cudaGetLastError();
+}
+
+// Source injection of one step (Xt_add_wavelet_sxyz x2, ose_3d_lib.cu:610-633):
+// the step index lives in device memory (ctr[0] = next step, ctr[1] = current)
+// so a captured graph can replay it.
+__global__ void k_inject(float2* W, long long src, const float* ricker, const float* hil, int* ctr, int nt)
+{
+    const int it = ctr[0];
+    ctr[1] = it;
+    ctr[0] = it + 1;
+    if (it >= 0 && it < nt) {
+        float2 w = W[src];
+        w.x += ricker[it];
+        w.y += hil[it];
+        W[src] = w;
+    }
+}
+
+cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float* ricker,
+                          const float* hil, int* ctr, int nt)
+{
+    k_inject<<<1, 1, 0, s>>>(W, src, ricker, hil, ctr, nt);
+    return cudaGetLastError();
+}
+
+}  // namespace ose

@@ -1,0 +1,267 @@
+"""Python binding of libose3d.so (ctypes over the C ABI of include/ose3d.h).
+
+The class mirrors the reference program's flow (ose_3d.cu:145-304): create
+(Alloc + model + sponge + plan), reset_shot (Xtdata_value + Alloc_wavelet),
+step (inject + wavefield_extro_ori2 + record), run (the time loop), and the
+output writers.  There is no CPU fallback: if the library or a GPU is missing,
+loading or creating raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libose3d.so")
+
+OK = 0
+FIELD_P, FIELD_Q, FIELD_V = 0, 1, 2
+LAYOUT_ZYX, LAYOUT_YXZ = 0, 1
+SPONGE_REFERENCE, SPONGE_CERJAN = 0, 1
+
+STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOMEM",
+          4: "OSE_ERR_IO", 5: "OSE_ERR_UNSUPPORTED", 6: "OSE_ERR_STATE", 7: "OSE_ERR_NUMERIC"}
+
+# Every symbol include/ose3d.h declares.
+EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_from_file",
+           "ose_destroy", "ose_last_error", "ose_get_derived", "ose_reset_shot", "ose_step",
+           "ose_run", "ose_run_record", "ose_run_timed", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
+           "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
+           "ose_profile_step", "ose_write_outputs", "ose_version"]
+
+
+class OseError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    """ose_params (include/ose3d.h)."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("bu", ctypes.c_int), ("bd", ctypes.c_int), ("bl", ctypes.c_int),
+        ("br", ctypes.c_int), ("bf", ctypes.c_int), ("bb", ctypes.c_int),
+        ("nt", ctypes.c_int),
+        ("fm", ctypes.c_float), ("dt", ctypes.c_float), ("amp", ctypes.c_float),
+        ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
+        ("nshot", ctypes.c_int),
+        ("sxbeg", ctypes.c_int), ("sybeg", ctypes.c_int), ("szbeg", ctypes.c_int),
+        ("jsx", ctypes.c_int), ("jsy", ctypes.c_int), ("jsz", ctypes.c_int),
+        ("gxbeg", ctypes.c_int), ("gybeg", ctypes.c_int), ("gzbeg", ctypes.c_int),
+        ("jgx", ctypes.c_int), ("jgy", ctypes.c_int), ("jgz", ctypes.c_int),
+        ("csdgather", ctypes.c_int),
+        ("sponge_mode", ctypes.c_int), ("cerjan_factor", ctypes.c_float),
+        ("hilbert_div_nt", ctypes.c_int), ("M_override", ctypes.c_int),
+    ]
+
+
+class Derived(ctypes.Structure):
+    """ose_derived (include/ose3d.h)."""
+
+    _fields_ = [
+        ("nxb", ctypes.c_int), ("nyb", ctypes.c_int), ("nzb", ctypes.c_int),
+        ("br", ctypes.c_int), ("bb", ctypes.c_int), ("bd", ctypes.c_int),
+        ("ng", ctypes.c_int), ("M", ctypes.c_int), ("vmax", ctypes.c_float),
+        ("R", ctypes.c_double), ("dtR", ctypes.c_double),
+        ("dkx", ctypes.c_double), ("dky", ctypes.c_double), ("dkz", ctypes.c_double),
+        ("bessel_tail", ctypes.c_double), ("device_bytes", ctypes.c_size_t),
+        ("path", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libose3d.so and declare every entry point.  Raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"libose3d.so not built ({path}); run 3d-ose_gb300/build.py")
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    H = ctypes.c_void_p
+    f32 = P(ctypes.c_float)
+    sig = {
+        "ose_default_params": ([P(Params)], ctypes.c_int),
+        "ose_padded_dims": ([P(Params), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
+        "ose_create": ([P(Params), f32, P(H)], ctypes.c_int),
+        "ose_create_from_file": ([P(Params), ctypes.c_char_p, P(H)], ctypes.c_int),
+        "ose_destroy": ([H], ctypes.c_int),
+        "ose_last_error": ([H], ctypes.c_char_p),
+        "ose_get_derived": ([H, P(Derived)], ctypes.c_int),
+        "ose_reset_shot": ([H, ctypes.c_int], ctypes.c_int),
+        "ose_step": ([H], ctypes.c_int),
+        "ose_run": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_run_record": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_run_timed": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_get_it": ([H, P(ctypes.c_int)], ctypes.c_int),
+        "ose_get_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
+        "ose_set_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
+        "ose_get_gather": ([H, f32], ctypes.c_int),
+        "ose_get_wavelets": ([H, f32, f32], ctypes.c_int),
+        "ose_get_sponge": ([H, f32, f32, f32], ctypes.c_int),
+        "ose_apply_operator": ([H, f32, f32], ctypes.c_int),
+        "ose_profile_step": ([H, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), P(ctypes.c_char_p),
+                              f32, P(ctypes.c_double), P(ctypes.c_int)], ctypes.c_int),
+        "ose_write_outputs": ([H, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
+        "ose_version": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def default_params(**kw) -> Params:
+    """The reference main()'s hard-coded parameters (ose_3d.cu:75-118), overridden by keyword."""
+    p = Params()
+    load_library().ose_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _f32(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Modeler:
+    """One shot-at-a-time OSE modeler on the current CUDA device."""
+
+    def __init__(self, params: Params, vel_xyz: np.ndarray):
+        self._lib = load_library()
+        self.params = params
+        v = np.ascontiguousarray(vel_xyz, dtype=np.float32)
+        if v.size != params.nx * params.ny * params.nz:
+            raise ValueError("velocity model must hold nx*ny*nz values ([x][y][z])")
+        h = ctypes.c_void_p()
+        st = self._lib.ose_create(ctypes.byref(params), _f32(v), ctypes.byref(h))
+        if st != OK:
+            raise OseError(st, self._lib.ose_last_error(None).decode())
+        self._h = h
+        self.derived = Derived()
+        self._check(self._lib.ose_get_derived(self._h, ctypes.byref(self.derived)))
+        d = self.derived
+        self.shape = (d.nzb, d.nyb, d.nxb)
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ose_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != OK:
+            raise OseError(st, self._lib.ose_last_error(self._h).decode())
+
+    # -- time loop ----------------------------------------------------------
+    def reset_shot(self, shot: int = 0):
+        self._check(self._lib.ose_reset_shot(self._h, shot))
+
+    def step(self):
+        self._check(self._lib.ose_step(self._h))
+
+    def run(self, nsteps: int, want_gather: bool = False):
+        """nsteps steps by graph replay; returns the [ig][it] gather if asked."""
+        if want_gather:
+            g = np.zeros((self.derived.ng, self.params.nt), np.float32)
+            self._check(self._lib.ose_run(self._h, nsteps, _f32(g)))
+            return g
+        self._check(self._lib.ose_run(self._h, nsteps, None))
+        return None
+
+    def run_record(self, nsteps: int, out: np.ndarray | None = None) -> np.ndarray:
+        """nsteps steps, returning their receiver rows [it][ig] (copied every step)."""
+        if out is None:
+            out = np.zeros((nsteps, self.derived.ng), np.float32)
+        self._check(self._lib.ose_run_record(self._h, nsteps, _f32(out)))
+        return out
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = ctypes.c_float()
+        self._check(self._lib.ose_run_timed(self._h, nsteps, ctypes.byref(ms)))
+        return ms.value
+
+    @property
+    def it(self) -> int:
+        v = ctypes.c_int()
+        self._check(self._lib.ose_get_it(self._h, ctypes.byref(v)))
+        return v.value
+
+    # -- data in and out ----------------------------------------------------
+    def gather(self) -> np.ndarray:
+        """[ig][it], ng x nt (the qshot2.bin order)."""
+        g = np.zeros((self.derived.ng, self.params.nt), np.float32)
+        self._check(self._lib.ose_get_gather(self._h, _f32(g)))
+        return g
+
+    def wavefield(self, which: int = FIELD_Q, layout: int = LAYOUT_ZYX) -> np.ndarray:
+        d = self.derived
+        out = np.zeros(d.nxb * d.nyb * d.nzb, np.float32)
+        self._check(self._lib.ose_get_wavefield(self._h, which, _f32(out), layout))
+        return out.reshape(self.shape if layout == LAYOUT_ZYX else (d.nyb, d.nxb, d.nzb))
+
+    def set_wavefield(self, which: int, data: np.ndarray, layout: int = LAYOUT_ZYX):
+        a = np.ascontiguousarray(data, dtype=np.float32)
+        self._check(self._lib.ose_set_wavefield(self._h, which, _f32(a), layout))
+
+    def wavelets(self):
+        nt = self.params.nt
+        r, h = np.zeros(nt, np.float32), np.zeros(nt, np.float32)
+        self._check(self._lib.ose_get_wavelets(self._h, _f32(r), _f32(h)))
+        return r, h
+
+    def sponge(self):
+        d = self.derived
+        ax, ay, az = (np.zeros(n, np.float32) for n in (d.nxb, d.nyb, d.nzb))
+        self._check(self._lib.ose_get_sponge(self._h, _f32(ax), _f32(ay), _f32(az)))
+        return ax, ay, az
+
+    def apply_operator(self, x: np.ndarray) -> np.ndarray:
+        """v * IFFT3(|k| FFT3(x)) / (R N) on a complex64 [nzb][nyb][nxb] field."""
+        a = np.ascontiguousarray(x, dtype=np.complex64)
+        out = np.zeros_like(a)
+        self._check(self._lib.ose_apply_operator(self._h, _f32(a.view(np.float32)),
+                                                 _f32(out.view(np.float32))))
+        return out
+
+    def profile_step(self, reps: int = 1):
+        cap = 8
+        count = ctypes.c_int()
+        names = (ctypes.c_char_p * cap)()
+        ms = np.zeros(cap, np.float32)
+        by = np.zeros(cap, np.float64)
+        lps = ctypes.c_int()
+        self._check(self._lib.ose_profile_step(self._h, reps, cap, ctypes.byref(count), names,
+                                               _f32(ms), by.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               ctypes.byref(lps)))
+        rows = [dict(name=names[i].decode(), ms=float(ms[i]), bytes=float(by[i]))
+                for i in range(count.value)]
+        return rows, lps.value
+
+    def write_outputs(self, gather_path: str | None, par_path: str | None):
+        self._check(self._lib.ose_write_outputs(
+            self._h, gather_path.encode() if gather_path else None,
+            par_path.encode() if par_path else None))

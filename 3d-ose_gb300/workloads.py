@@ -1,0 +1,63 @@
+"""Seeded synthetic workloads of the benchmark configurations (velocity model in
+the reference layout [x][y][z], float32, plus the modeler parameters).
+
+No public dataset is involved: each model is generated from a fixed seed with
+the shapes, sizes and value ranges the configuration names.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def smooth_random_salt(nx: int, ny: int, nz: int, seed: int = 2024, vmin: float = 1500.0,
+                       vmax: float = 4500.0, sigma: float = 6.0) -> np.ndarray:
+    """Gaussian-smoothed random field rescaled to [vmin, vmax], increasing on
+    average with depth, with a salt-like ellipsoid at vmax."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    f = gaussian_filter(rng.standard_normal((nx, ny, nz)), sigma=sigma, mode="wrap")
+    f = (f - f.min()) / max(f.max() - f.min(), 1e-12)
+    depth = np.linspace(0.0, 1.0, nz)[None, None, :]
+    v = vmin + (vmax - vmin) * np.clip(0.6 * depth + 0.4 * f, 0.0, 1.0)
+    x, y, z = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ell = (((x - 0.5 * nx) / (0.22 * nx)) ** 2 + ((y - 0.55 * ny) / (0.18 * ny)) ** 2 +
+           ((z - 0.6 * nz) / (0.12 * nz)) ** 2) <= 1.0
+    v[ell] = vmax
+    return np.ascontiguousarray(v, dtype=np.float32)
+
+
+def layered_perturbed(nx: int, ny: int, nz: int, seed: int = 7) -> np.ndarray:
+    """Four horizontal layers 1500/2200/3000/3800 m/s at depth quarters times
+    (1 + d), d a Gaussian-smoothed (sigma = 3 cells) normal field scaled to
+    max |d| = 0.05."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    z = np.arange(nz)
+    base = np.choose(np.minimum(4 * z // nz, 3), [1500.0, 2200.0, 3000.0, 3800.0])
+    d = gaussian_filter(rng.standard_normal((nx, ny, nz)), sigma=3.0, mode="nearest")
+    d *= 0.05 / np.abs(d).max()
+    return np.ascontiguousarray(base[None, None, :] * (1.0 + d), dtype=np.float32)
+
+
+# name -> (model builder, modeler parameters)
+CONFIGS = {
+    # Plain OSE, FP32, padded 256^3 = interior 196^3 + 30-cell sponge, 25 Hz Ricker
+    # near the surface centre, dt 2 ms, 2000 steps, full-surface receivers.
+    "ose256": (lambda: smooth_random_salt(196, 196, 196),
+               dict(nx=196, ny=196, nz=196, bu=30, bd=30, bl=30, br=30, bf=30, bb=30, nt=2000,
+                    fm=25.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                    sxbeg=98, sybeg=98, szbeg=5, gzbeg=0)),
+    # Non-power-of-two variant: padded 320 x 288 x 256.
+    "ose320x288x256": (lambda: smooth_random_salt(260, 228, 196, seed=2025),
+                       dict(nx=260, ny=228, nz=196, bu=30, bd=30, bl=30, br=30, bf=30, bb=30,
+                            nt=2000, fm=25.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                            sxbeg=130, sybeg=114, szbeg=5, gzbeg=0)),
+    # Interior 101^3 + 20-cell sponge (padded 142^3), 20 Hz at (50,50,10), 1000 steps,
+    # receivers at z = 5.
+    "ose142": (lambda: layered_perturbed(101, 101, 101),
+               dict(nx=101, ny=101, nz=101, bu=20, bd=20, bl=20, br=20, bf=20, bb=20, nt=1000,
+                    fm=20.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                    sxbeg=50, sybeg=50, szbeg=10, gzbeg=5)),
+}

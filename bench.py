@@ -1,0 +1,284 @@
+#!/usr/bin/env python3
+"""Benchmark of the plain FP32 OSE time step on GB300 (one JSON line on rank 0).
+
+A step is one OSE time step (source injection, M+1 operator applications with
+the fused series update, receiver row) of the padded 256^3 workload
+(interior 196^3 + 30-cell sponge, seeded smooth random 1500-4500 m/s model with
+a 4500 m/s salt ellipsoid, 25 Hz Ricker, dt = 2 ms).  Inputs stay resident in
+HBM; every field (134 MB) is larger than L2, so no L2 flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same step (the oracle, FP64,
+all host threads) on a bounded sample; the reference program itself has no
+CPU path and its multi-GPU cuFFT-Xt path needs two GPUs.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "3d-ose_gb300")
+for p in (PKG, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "Gcell-steps/s at 256³ vs plain OSE at ≤1e-4 rel-L2 vs FP64; % HBM roofline"
+UNIT = "Gcell-steps/s"
+WORKLOAD = "ose256"
+WORKLOAD_TEXT = ("plain OSE FP32 time step, padded 256x256x256 (interior 196^3 + 30-cell sponge), "
+                 "M=10 (11 operator applications), 25 Hz Ricker near the surface centre, dt 2 ms, "
+                 "full-surface receiver gather")
+DATA = "synthetic: seeded smooth random 1500-4500 m/s model with a 4500 m/s salt ellipsoid"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (gloo, host tensors)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def device_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except Exception:
+        pass
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        rows = [r for r in csv.reader(io.StringIO(open(self.path).read())) if len(r) >= 9]
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(WORKLOAD, {}).get(kernel)
+    except Exception:
+        return None
+
+
+def oracle_rate(kw, vel, nsteps: int):
+    """Gcell-steps/s of the FP64 oracle over nsteps full-size steps (setup excluded)."""
+    import oracle as O
+    O.build()
+    p = O.make_params(**kw)
+    d = O.derive(p)
+    t0 = time.perf_counter()
+    O.run(p, vel, 0)
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.run(p, vel, nsteps)
+    t = time.perf_counter() - t0 - t_setup
+    cells = d.nxb * d.nyb * d.nzb
+    return cells * nsteps / max(t, 1e-9) / 1e9, O.threads(), t
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    import workloads
+    build, kw = workloads.CONFIGS[WORKLOAD]
+    vel = build()
+    nsteps = max(1, min(args.steps, 2))
+    value, cores, t = oracle_rate(kw, vel, nsteps)
+    sample = (f"{nsteps} full-size step(s) of the {WORKLOAD} workload on the FP64 CPU oracle "
+              f"(the reference has no CPU path of its own), {t:.1f} s")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * t / nsteps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": {"workload": WORKLOAD, "text": WORKLOAD_TEXT},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist(world)
+
+    import numpy as np
+    import __graft_entry__ as ge
+    ge.build_library()
+    import ose3d
+    import workloads
+
+    build, kw = workloads.CONFIGS[WORKLOAD]
+    vel = build()
+    warm = max(3, args.warmup)
+    if warm + args.steps + 1 > kw["nt"]:
+        raise SystemExit(f"steps + warmup must stay below nt = {kw['nt']}")
+    params = ose3d.default_params(**kw)
+    m = ose3d.Modeler(params, vel)
+    d = m.derived
+    cells = d.nxb * d.nyb * d.nzb
+    m.reset_shot(rank)
+    m.run(warm)
+
+    dist.barrier()
+    device_sync()
+    clk = ClockSampler()
+    clk.start()
+    ms = m.run_timed(args.steps)
+    clocks = clk.stop()
+    device_sync()
+    dist.barrier()
+    ms = dist.max(ms)
+    value = world * cells * args.steps / (ms * 1e-3) / 1e9
+
+    # per-kernel launch durations (events bracketing each launch, one step)
+    rows, launches_per_step = m.profile_step(reps=2)
+    per_step = {r["name"]: (d.M + 1 if r["name"] != "inject" else 1) for r in rows}
+    share = {r["name"]: r["ms"] * per_step[r["name"]] for r in rows}
+    total = sum(share.values())
+    dom = max(rows, key=lambda r: share[r["name"]])
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": ncu_traffic(dom["name"]),
+                "algorithmic_bytes_per_launch": dom["bytes"], "ms_per_launch": dom["ms"],
+                "kernel_shares": {k: v / total for k, v in share.items()},
+                "step_bytes_model": sum(r["bytes"] * per_step[r["name"]] for r in rows) / cells,
+                "step_achieved_gbs": sum(r["bytes"] * per_step[r["name"]] for r in rows) /
+                (ms * 1e-3 / args.steps) / 1e9}
+    m.close()
+
+    # end to end through the C ABI from host buffers: create (model upload),
+    # reset (wavelets), K steps each copying its receiver row to the host,
+    # final P and Q back to the host
+    device_sync()
+    t0 = time.perf_counter()
+    m2 = ose3d.Modeler(params, vel)
+    m2.reset_shot(rank)
+    rows_out = m2.run_record(args.steps)
+    q = m2.wavefield(ose3d.FIELD_Q)
+    p_ = m2.wavefield(ose3d.FIELD_P)
+    t_e2e = time.perf_counter() - t0
+    m2.close()
+    t_e2e = dist.max(t_e2e)
+    h2d = (vel.nbytes + 2 * 4 * kw["nt"]) / args.steps
+    d2h = (rows_out.nbytes + q.nbytes + p_.nbytes) / args.steps
+    e2e = {"value": world * cells * args.steps / t_e2e / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "timing": "host wall clock around create + reset_shot + run_record + wavefield reads"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, t = oracle_rate(kw, vel, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"1 full-size {WORKLOAD} step on the FP64 CPU oracle ({t:.1f} s)"}
+    dist.close()
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": DATA,
+            "config": {"workload": WORKLOAD, "text": WORKLOAD_TEXT, "grid": [d.nxb, d.nyb, d.nzb],
+                       "M": d.M, "kernel_path": "generic" if d.path == 0 else "plane",
+                       "l2": "inputs larger than L2 (each field 134 MB; 0.6 GB resident)",
+                       "parallelism": f"replicas x{world} (one independent shot per GPU)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -148,6 +148,12 @@ ose_status ose_step(ose_handle* h);
  * with (ng,1,nt), ose_3d_lib.cu:327-343); rows of steps not run yet are 0. */
 ose_status ose_run(ose_handle* h, int nsteps, float* gather_out);
 
+/* nsteps steps, copying each step's receiver row to the host as the
+ * reference's loop does (rec_shotdata_3d + cudaMemcpy of ng floats +
+ * rec_slice_to_data, ose_3d.cu:271-274).  rows_out receives nsteps x ng
+ * floats in step order [it][ig] (the rows of those steps only). */
+ose_status ose_run_record(ose_handle* h, int nsteps, float* rows_out);
+
 /* As ose_run, but times the device work with CUDA events on the handle's
  * stream and copies nothing back.  *ms receives the elapsed device time. */
 ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms);

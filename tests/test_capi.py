@@ -1,0 +1,73 @@
+"""The C ABI library without a GPU: it loads, exports every entry point that
+include/ose3d.h declares, and its host-only calls agree with the oracle."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+import ose3d
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "ose3d.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ose_[a-z_0-9]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as ge
+    ge.build_library()
+    return ose3d.load_library()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    assert sorted(ose3d.EXPORTS) == syms
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_default_params_are_the_reference_main(lib):
+    p = ose3d.default_params()
+    assert (p.nx, p.ny, p.nz, p.bu, p.nt) == (101, 101, 101, 25, 300)
+    assert abs(p.fm - 40.0) < 1e-6 and abs(p.dt - 0.001) < 1e-9 and abs(p.amp - 100.0) < 1e-6
+    assert (p.sxbeg, p.sybeg, p.szbeg) == (50, 50, 0)
+
+
+@pytest.mark.parametrize("dims", [(101, 101, 101, 25, 25), (20, 18, 16, 6, 5), (100, 101, 102, 25, 26),
+                                  (196, 196, 196, 30, 30), (7, 1, 3, 0, 0)])
+def test_padded_dims_match_oracle(lib, dims):
+    nx, ny, nz, b0, b1 = dims
+    p = ose3d.default_params(nx=nx, ny=ny, nz=nz, bl=b0, br=b1, bf=b0, bb=b1, bu=b0, bd=b1)
+    out = [ctypes.c_int() for _ in range(3)]
+    assert lib.ose_padded_dims(ctypes.byref(p), *[ctypes.byref(o) for o in out]) == 0
+    d = O.derive(O.make_params(nx=nx, ny=ny, nz=nz, bl=b0, br=b1, bf=b0, bb=b1, bu=b0, bd=b1))
+    assert [o.value for o in out] == [d.nxb, d.nyb, d.nzb]
+    assert all(o.value % 2 == 0 for o in out)
+
+
+def test_invalid_params_rejected(lib):
+    p = ose3d.default_params(nx=0)
+    out = [ctypes.c_int() for _ in range(3)]
+    assert lib.ose_padded_dims(ctypes.byref(p), *[ctypes.byref(o) for o in out]) == 1
+    assert b"nx" in lib.ose_last_error(None)
+
+
+def test_null_handle_calls_are_errors(lib):
+    assert lib.ose_step(None) == 1
+    assert lib.ose_reset_shot(None, 0) == 1
+    assert lib.ose_destroy(None) == 0
+    assert lib.ose_version().startswith(b"ose3d")
+
+
+def test_python_class_mirrors_header_structs():
+    assert ctypes.sizeof(ose3d.Params) == ctypes.sizeof(O.OseParams)
+    assert [f[0] for f in ose3d.Params._fields_] == [f[0] for f in O.OseParams._fields_]
+    assert [f[0] for f in ose3d.Derived._fields_] == [f[0] for f in O.OseDerived._fields_]

@@ -1,0 +1,143 @@
+"""CUDA path (libose3d.so through its C ABI) against the reference goldens and
+the FP64 oracle.  Tolerance: 1e-4 relative L2 for gathers and wavefields
+(FP32 path vs FP64 / reference); receiver order is exact by construction and
+checked through the per-trace comparison."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import ose3d
+from golden_util import CASES, load, model_of, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as ge
+    ge.build_library()
+    ose3d.load_library()
+
+
+def gpu_params(g):
+    p = dict(g["params"])
+    p.pop("nsteps")
+    return p
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_time_loop_matches_reference_goldens(name):
+    g = load(name)
+    kw = gpu_params(g)
+    ns = g["params"]["nsteps"]
+    with ose3d.Modeler(ose3d.default_params(**kw), model_of(g)) as m:
+        assert [m.derived.nxb, m.derived.nyb, m.derived.nzb] == list(g["dims"])
+        assert m.derived.M == int(g["M"])
+        m.reset_shot(0)
+        r, h = m.wavelets()
+        assert np.max(np.abs(r - g["ricker"])) <= 1e-6 * np.abs(g["ricker"]).max()
+        assert np.max(np.abs(h - g["hilbert"])) <= 2e-6 * np.abs(g["hilbert"]).max()
+        ax, ay, az = m.sponge()
+        assert np.max(np.abs(ax - g["att_x"])) <= 2e-7
+        gather = m.run(ns, want_gather=True)          # [ig][it]
+        P = m.wavefield(ose3d.FIELD_P)
+        Q = m.wavefield(ose3d.FIELD_Q)
+    ref = g["gather"].T                                  # [ig][it]
+    assert rel_l2(gather[:, :ns], ref) < TOL
+    assert np.all(gather[:, ns:] == 0)
+    # per-trace check: every receiver's trace matches its own reference trace
+    tr_err = np.linalg.norm(gather[:, :ns] - ref, axis=1) / (np.linalg.norm(ref, axis=1) + 1e-30)
+    big = np.linalg.norm(ref, axis=1) > 1e-3 * np.linalg.norm(ref, axis=1).max()
+    assert np.all(tr_err[big] < 10 * TOL)
+    if "Q" in g:
+        assert rel_l2(P, g["P"]) < TOL
+        assert rel_l2(Q, g["Q"]) < TOL
+    else:
+        zs, ys = g["plane_index"]
+        assert rel_l2(Q[zs], g["Q_plane_z"]) < TOL
+        assert rel_l2(P[:, ys], g["P_plane_y"]) < TOL
+        assert abs(np.linalg.norm(Q.astype(np.float64)) / g["Q_norm"] - 1) < TOL
+
+
+@pytest.mark.parametrize("dims", [(20, 18, 16, 6), (9, 13, 11, 5), (40, 24, 30, 8)])
+def test_operator_matches_oracle(dims):
+    nx, ny, nz, b = dims
+    rng = np.random.default_rng(nx * 100 + ny)
+    kw = dict(nx=nx, ny=ny, nz=nz, bu=b, bd=b, bl=b, br=b, bf=b, bb=b, nt=8)
+    vel = (1500 + 3000 * rng.random((nx, ny, nz))).astype(np.float32)
+    with ose3d.Modeler(ose3d.default_params(**kw), vel) as m:
+        x = (rng.standard_normal(m.shape) + 1j * rng.standard_normal(m.shape)).astype(np.complex64)
+        y = m.apply_operator(x)
+        vb = m.wavefield(ose3d.FIELD_V)
+        R = m.derived.R
+    op = O.make_params(**kw)
+    ref = O.apply_operator(op, vb, R, x.astype(np.complex128))
+    assert rel_l2(y, ref) < 2e-6
+
+
+def test_graph_replay_equals_single_steps():
+    g = load("small_judge_odd")
+    kw = gpu_params(g)
+    vel = model_of(g)
+    with ose3d.Modeler(ose3d.default_params(**kw), vel) as a, ose3d.Modeler(ose3d.default_params(**kw), vel) as b:
+        a.reset_shot(0)
+        b.reset_shot(0)
+        for _ in range(10):
+            a.step()
+        b.run(4)
+        b.run(6)
+        assert a.it == b.it == 10
+        assert np.array_equal(a.wavefield(ose3d.FIELD_Q), b.wavefield(ose3d.FIELD_Q))
+        assert np.array_equal(a.gather(), b.gather())
+
+
+def test_switches_match_oracle():
+    """Cerjan sponge, Q trace divided by nt, receivers at depth 3, fixed M, second shot."""
+    rng = np.random.default_rng(11)
+    kw = dict(nx=18, ny=14, nz=20, bu=5, bd=6, bl=7, br=4, bf=5, bb=5, nt=40, fm=35.0, dt=0.0012,
+              amp=10.0, sxbeg=4, sybeg=6, szbeg=3, jsx=3, jsy=1, jsz=2, gzbeg=3,
+              sponge_mode=1, cerjan_factor=0.05, hilbert_div_nt=1, M_override=9)
+    vel = (2200 + 1200 * rng.random((18, 14, 20))).astype(np.float32)
+    with ose3d.Modeler(ose3d.default_params(**kw), vel) as m:
+        assert m.derived.M == 9
+        m.reset_shot(2)
+        gather = m.run(30, want_gather=True)
+        Q = m.wavefield(ose3d.FIELD_Q)
+        P = m.wavefield(ose3d.FIELD_P)
+    og, oP, oQ = O.run(O.make_params(**kw), vel, 30, shot=2)
+    assert rel_l2(gather[:, :30], og.T) < TOL
+    assert rel_l2(Q, oQ) < TOL
+    assert rel_l2(P, oP) < TOL
+
+
+def test_state_errors():
+    g = load("small_judge_odd")
+    kw = gpu_params(g)
+    with ose3d.Modeler(ose3d.default_params(**kw), model_of(g)) as m:
+        with pytest.raises(ose3d.OseError) as e:
+            m.step()
+        assert e.value.status == 6
+        m.reset_shot(0)
+        with pytest.raises(ose3d.OseError) as e:
+            m.run(kw["nt"] + 1)
+        assert e.value.status == 1
+    with pytest.raises(ose3d.OseError) as e:
+        ose3d.Modeler(ose3d.default_params(**kw), -model_of(g))
+    assert e.value.status == 1
+
+
+def test_linearity_in_source_amplitude():
+    """The step is linear in the source: doubling amp doubles the gather."""
+    g = load("small_deep_source_odd_nt")
+    kw = gpu_params(g)
+    vel = model_of(g)
+    out = []
+    for amp in (1.0, 2.0):
+        kw["amp"] = amp
+        with ose3d.Modeler(ose3d.default_params(**kw), vel) as m:
+            m.reset_shot(0)
+            out.append(m.run(25, want_gather=True))
+    assert rel_l2(out[1], 2.0 * out[0]) < 1e-6
