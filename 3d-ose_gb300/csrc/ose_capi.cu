@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -102,21 +103,90 @@ void free_all(ose_handle* h)
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
+// Runs one launch; with a timing record, brackets it with events and adds
+// its duration and algorithmic bytes to class cls.
+template <typename F>
+cudaError_t timed(ose::KernelTiming* tm, cudaStream_t s, int cls, double bytes, F launch)
+{
+    if (tm) cudaEventRecord(tm->ev[0], s);
+    cudaError_t e = launch();
+    if (tm && e == cudaSuccess) {
+        cudaEventRecord(tm->ev[1], s);
+        e = cudaEventSynchronize(tm->ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[1]);
+        tm->ms[cls] += ms;
+        tm->count[cls] += 1;
+        tm->bytes[cls] += bytes;
+    }
+    return e;
+}
+
+// Plane path step: 2 HBM passes per operator application (ose_plane.cu).
+// Timing classes: 0 plane_fwd, 1 zpass, 2 plane_inv_first, 3 plane_inv_mid,
+// 4 plane_inv_last, 5 inject.
+cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
+{
+    cudaStream_t s = h->stream;
+    const double N = (double)h->g.ncell;
+    cudaError_t e = timed(tm, s, 5, 16.0, [&] {
+        return ose::launch_inject(s, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
+    });
+    if (e != cudaSuccess) return e;
+    const int M = h->d.M;
+    ose::EpiArgs ea{};
+    ea.vs = h->vs;
+    ea.ax = h->ax;
+    ea.ay = h->ay;
+    ea.az = h->az;
+    ea.S = h->S;
+    ea.wout = h->W;
+    ea.gather = h->gather;
+    ea.cur = h->ctr + 1;
+    ea.gz = h->p.bu + h->p.gzbeg;
+    ea.bl = h->p.bl;
+    ea.bf = h->p.bf;
+    ea.nx = h->p.nx;
+    ea.ny = h->p.ny;
+    ea.nt = h->p.nt;
+    e = timed(tm, s, 0, 16.0 * N, [&] { return ose::launch_plane_fwd(s, h->W, h->X, h->twx); });
+    if (e != cudaSuccess) return e;
+    for (int n = 0; n <= M; ++n) {
+        e = timed(tm, s, 1, 16.0 * N, [&] { return ose::launch_zpass(s, h->X, h->twx, h->tables); });
+        if (e != cudaSuccess) return e;
+        ose::EpiMode mode;
+        double bytes;
+        int cls;
+        if (n == 0) {
+            ea.prev = h->A;
+            ea.w = h->W;
+            ea.c0 = (float)h->J[0];
+            ea.c1 = (float)(2.0 * h->J[1]);
+            mode = ose::EPI_FIRST;
+            bytes = (M > 0 ? 44.0 : 36.0) * N;
+            cls = 2;
+        } else {
+            ea.prev = (n & 1) ? h->W : h->A;
+            ea.c1 = (float)(2.0 * h->J[n + 1]);
+            mode = n == M ? ose::EPI_LAST : ose::EPI_MID;
+            bytes = (n == M ? 36.0 : 52.0) * N;
+            cls = n == M ? 4 : 3;
+        }
+        const bool fwd = n < M;
+        e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->twx, ea); });
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Enqueue one whole time step on h->stream (no synchronisation).
 cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
 {
+    if (h->d.path == OSE_PATH_PLANE) return enqueue_step_plane(h, tm);
     cudaError_t e;
-    if (tm) cudaEventRecord(tm->ev[0], h->stream);
-    e = ose::launch_inject(h->stream, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
-    if (tm) {
-        cudaEventRecord(tm->ev[1], h->stream);
-        cudaEventSynchronize(tm->ev[1]);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[1]);
-        tm->ms[5] += ms;
-        tm->count[5] += 1;
-        tm->bytes[5] += 16.0;
-    }
+    e = timed(tm, h->stream, 5, 16.0, [&] {
+        return ose::launch_inject(h->stream, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
+    });
     if (e != cudaSuccess) return e;
     const int M = h->d.M;
     ose::EpiArgs ea{};
@@ -313,6 +383,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
         }                                                                           \
     } while (0)
     CKC(ose::configure_kernels());
+    CKC(ose::configure_plane_kernels());
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
@@ -356,7 +427,9 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     h->tables.kx2 = h->kx2;
     h->tables.ky2 = h->ky2;
     h->tables.kz2 = h->kz2;
-    d.path = OSE_PATH_GENERIC;
+    d.path = ose::plane_path_supported(d.nxb, d.nyb, d.nzb) ? OSE_PATH_PLANE : OSE_PATH_GENERIC;
+    if (const char* env = getenv("OSE3D_PATH"))
+        if (!strcmp(env, "generic")) d.path = OSE_PATH_GENERIC;
     d.device_bytes = h->bytes;
     *out = h;
     return OSE_OK;
@@ -483,6 +556,18 @@ ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms)
     return OSE_OK;
 }
 
+ose_status ose_select_path(ose_handle* h, int path)
+{
+    if (!h) return OSE_ERR_INVALID;
+    if (path == OSE_PATH_PLANE && !ose::plane_path_supported(h->d.nxb, h->d.nyb, h->d.nzb))
+        return fail(h, OSE_ERR_UNSUPPORTED, "the plane path needs a 256 x 256 x 256 padded grid");
+    if (path != OSE_PATH_PLANE && path != OSE_PATH_GENERIC) return fail(h, OSE_ERR_INVALID, "unknown path");
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    h->d.path = path;
+    return OSE_OK;
+}
+
 ose_status ose_get_it(const ose_handle* h, int* it)
 {
     if (!h || !it) return OSE_ERR_INVALID;
@@ -563,7 +648,10 @@ ose_status ose_apply_operator(ose_handle* h, const float* in, float* out)
     const size_t N = (size_t)h->g.ncell;
     // A and S carry no state between steps, so they serve as in/out here.
     CK(h, cudaMemcpyAsync(h->A, in, sizeof(float2) * N, cudaMemcpyHostToDevice, h->stream));
-    CK(h, ose::launch_apply_operator(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->A, h->X, h->S, h->vs));
+    if (h->d.path == OSE_PATH_PLANE)
+        CK(h, ose::launch_plane_apply_operator(h->stream, h->A, h->X, h->S, h->vs, h->twx, h->tables));
+    else
+        CK(h, ose::launch_apply_operator(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->A, h->X, h->S, h->vs));
     CK(h, cudaMemcpyAsync(out, h->S, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return OSE_OK;
@@ -576,8 +664,11 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
     if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
     if (h->it + reps > h->p.nt) return fail(h, OSE_ERR_INVALID, "reps beyond nt");
     ose::KernelTiming& t = h->timing;
-    static const char* kNames[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
-                                   "fft_x_inv_epilogue", "inject"};
+    static const char* kGeneric[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
+                                     "fft_x_inv_epilogue", "inject"};
+    static const char* kPlane[] = {"plane_fwd", "zpass", "plane_inv_first", "plane_inv_mid",
+                                   "plane_inv_last", "inject"};
+    const char** kNames = h->d.path == OSE_PATH_PLANE ? kPlane : kGeneric;
     const int nc = 6;
     for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
     for (int r = 0; r < reps; ++r) {

@@ -29,7 +29,7 @@ struct Geometry {
 
 // Epilogue selection of the last pass of one operator application
 // (wavefield_extro_ori2, ose_3d_lib.cu:651-870, fused).
-enum EpiMode { EPI_FIRST = 0, EPI_MID = 1, EPI_LAST = 2 };
+enum EpiMode { EPI_FIRST = 0, EPI_MID = 1, EPI_LAST = 2, EPI_SCALE = 3 };
 
 struct EpiArgs {
     float2* prev;         // FIRST: a_1 out.  MID/LAST: a_{n-1} in, a_{n+1} out (MID)
@@ -68,6 +68,17 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
                                   const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                   const float2* in, float2* X, float2* out, const float* vs);
 cudaError_t configure_kernels();
+
+// 256^3 fast path (ose_plane.cu).
+bool plane_path_supported(int nxb, int nyb, int nzb);
+cudaError_t configure_plane_kernels();
+cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const float2* tw);
+cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t);
+cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float2* Xin, float2* Xout,
+                             const float2* tw, const EpiArgs& e);
+cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
+                                        const float* vs, const float2* tw, const Tables& t);
+int plane_max_active_clusters();
 
 // Per-kernel-class timing used by ose_profile_step.
 struct KernelTiming {

@@ -129,7 +129,7 @@ __device__ float2* fft_lines(float2* a, float2* b, int L, int LS, int ES, bool l
     return a;
 }
 
-enum { EPI_NONE = -1, EPI_SCALE = 3 };
+enum { EPI_NONE = -1 };
 
 // The pointwise work of one application on cell i = (x, y, z); X is the
 // unnormalised inverse transform.

@@ -1,0 +1,516 @@
+// ose_plane.cu - the fast path for 256 x 256 x 256 padded grids.
+//
+// One operator application L = v * IFFT3(|k| FFT3(.)) / (R N) costs two HBM
+// passes here instead of five:
+//   k_zpass            z lines: forward FFT, * |k|, inverse FFT (in place)
+//   k_plane_inv<...>   one z plane per 8-CTA thread-block cluster: inverse y
+//                      and x FFTs, the step's pointwise update (the same
+//                      epilogue as the generic path: scal_vr_3d, the
+//                      recurrence, add_bessel_3d, apply_ABC_Xt, receivers),
+//                      then the NEXT application's forward x and y FFTs of the
+//                      new term, written as its spectrum.
+// plus k_plane_fwd (forward x and y FFTs of the state) once per step.
+//
+// Plane work is split over the cluster: CTA r owns rows y in [32r, 32r+32) for
+// the x transforms and columns x in [32r, 32r+32) for the y transforms; the
+// 512 KiB plane changes hands between the two through distributed shared
+// memory (each CTA's 64 KiB slice, read by the others with ld.shared::cluster).
+//
+// Every 256-point transform is a four-step 16 x 16 FFT: a line is held by 16
+// threads with 16 values each, a radix-16 DFT runs in registers, twiddles
+// W_256^(j k) come from a shared table, and one transpose through shared
+// memory connects the two radix-16 stages.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "ose_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace ose {
+namespace plane {
+
+constexpr int N = 256;          // line length on all three axes
+constexpr int CL = 8;           // CTAs per cluster (one plane per cluster)
+constexpr int SL = N / CL;      // rows / columns per CTA = 32
+constexpr int THREADS = 256;
+constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
+constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
+constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
+constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
+constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + N;   // + twiddle table
+constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX;
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b)   // a * conj(b)
+{
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+
+// times -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 rot(float2 a)
+{
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3)
+{
+    const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = rot<INV>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+// times W_16^E (forward) or its conjugate (inverse); E in {0,1,2,3,4,6,9}
+template <int E, bool INV>
+__device__ __forceinline__ float2 w16(float2 a)
+{
+    constexpr float C1 = 0.923879532511286756f;   // cos(pi/8)
+    constexpr float S1 = 0.382683432365089772f;   // sin(pi/8)
+    constexpr float H = 0.707106781186547524f;    // sqrt(1/2)
+    constexpr float s = INV ? 1.f : -1.f;         // sign of the sine part
+    if (E == 0) return a;
+    if (E == 4) return rot<INV>(a);
+    float c, sn;
+    if (E == 1) { c = C1; sn = s * S1; }
+    else if (E == 2) { c = H; sn = s * H; }
+    else if (E == 3) { c = S1; sn = s * C1; }
+    else if (E == 6) { c = -H; sn = s * H; }
+    else { c = -C1; sn = -s * S1; }   // E == 9
+    return make_float2(fmaf(a.x, c, -a.y * sn), fmaf(a.x, sn, a.y * c));
+}
+
+// In-register 16-point DFT, natural order in and out (4 x 4 split).
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&v)[16])
+{
+    // DFT4 over m1 for each m2 (elements m2, m2+4, m2+8, m2+12)
+#pragma unroll
+    for (int m2 = 0; m2 < 4; ++m2) dft4<INV>(v[m2], v[m2 + 4], v[m2 + 8], v[m2 + 12]);
+    // now v[m2 + 4 k1] = Y[m2][k1]; twiddle by W16^(m2 k1)
+    v[5] = w16<1, INV>(v[5]);
+    v[9] = w16<2, INV>(v[9]);
+    v[13] = w16<3, INV>(v[13]);
+    v[6] = w16<2, INV>(v[6]);
+    v[10] = w16<4, INV>(v[10]);
+    v[14] = w16<6, INV>(v[14]);
+    v[7] = w16<3, INV>(v[7]);
+    v[11] = w16<6, INV>(v[11]);
+    v[15] = w16<9, INV>(v[15]);
+    // DFT4 over m2 for each k1 (elements 4k1 .. 4k1+3) -> X[k1 + 4 k2] at v[4 k1 + k2]
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // transpose the 4 x 4 index (v[4 k1 + k2] -> v[k1 + 4 k2])
+    float2 t;
+    t = v[1]; v[1] = v[4]; v[4] = t;
+    t = v[2]; v[2] = v[8]; v[8] = t;
+    t = v[3]; v[3] = v[12]; v[12] = t;
+    t = v[6]; v[6] = v[9]; v[9] = t;
+    t = v[7]; v[7] = v[13]; v[13] = t;
+    t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+// Rows context (x transforms): slot s of thread t handles row
+// (warp + 8 s) * 2 + lane / 16 and line thread j = lane % 16.
+struct RowSlot {
+    int row, j;
+};
+__device__ __forceinline__ RowSlot row_slot(int s)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    return {(warp + 8 * s) * 2 + (lane >> 4), lane & 15};
+}
+// Columns context (y and z transforms): column c = lane, line thread j = warp + 8 s.
+struct ColSlot {
+    int c, j;
+};
+__device__ __forceinline__ ColSlot col_slot(int s)
+{
+    return {(int)(threadIdx.x & 31), (int)(threadIdx.x >> 5) + 8 * s};
+}
+
+// Exchange between the two radix-16 stages for both slots of every thread.
+// rows: buffer [row][a][TPAD]; cols: buffer [a][b][SL] (column fastest).
+template <bool ROWS>
+__device__ __forceinline__ void exchange(float2* T, float2 (&v0)[16], float2 (&v1)[16])
+{
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        float2(&v)[16] = s ? v1 : v0;
+        if (ROWS) {
+            const RowSlot q = row_slot(s);
+            float2* b = T + q.row * (16 * TPAD) + q.j * TPAD;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) b[k] = v[k];
+        } else {
+            const ColSlot q = col_slot(s);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) T[(q.j * 16 + k) * SL + q.c] = v[k];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        float2(&v)[16] = s ? v1 : v0;
+        if (ROWS) {
+            const RowSlot q = row_slot(s);
+            const float2* b = T + q.row * (16 * TPAD) + q.j;
+#pragma unroll
+            for (int a = 0; a < 16; ++a) v[a] = b[a * TPAD];
+        } else {
+            const ColSlot q = col_slot(s);
+#pragma unroll
+            for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + q.j) * SL + q.c];
+        }
+    }
+    __syncthreads();
+}
+
+// Four-step 256-point transform.  Forward: v[n1] = x[16 n1 + j] in,
+// v[k2] = X[j + 16 k2] out.  Inverse: the reverse.
+template <bool INV, bool ROWS>
+__device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)[16], float2 (&v1)[16])
+{
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        float2(&v)[16] = s ? v1 : v0;
+        const int j = ROWS ? row_slot(s).j : col_slot(s).j;
+        dft16<INV>(v);
+#pragma unroll
+        for (int k = 1; k < 16; ++k) v[k] = INV ? cmulc(v[k], tw[j * k]) : cmul(v[k], tw[j * k]);
+    }
+    exchange<ROWS>(T, v0, v1);
+    dft16<INV>(v0);
+    dft16<INV>(v1);
+}
+
+struct Args {
+    const float2* src;     // k_plane_fwd: state rows.  k_plane_inv: spectrum after k_zpass
+    float2* dst;           // spectrum of the next application (forward output)
+    const float2* tw;      // W_256^t, t < 256
+    const float* kx2;
+    const float* ky2;
+    const float* kz2;
+    EpiArgs e;
+};
+
+__device__ __forceinline__ void load_twiddles(float2* tw, const float2* g)
+{
+    for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = g[t];
+}
+
+// Forward x FFT of this CTA's 32 rows (values in v0/v1, spatial order) then
+// forward y FFT of its 32 columns; spectrum stored to dst plane z.
+__device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* smem, const float2* tw,
+                                           float2 (&v0)[16], float2 (&v1)[16], float2* dst, int z, int r)
+{
+    float2* T = smem;
+    fft256<false, true>(T, tw, v0, v1);
+    // natural-order rows into this CTA's slice A[row][kx]
+    float2* A = smem;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) A[q.row * N + q.j + 16 * k2] = v[k2];
+    }
+    cluster.sync();
+    // columns 32r..32r+31 of all 256 rows from the 8 slices
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) {
+            const float2* rem = cluster.map_shared_rank(A, n1 >> 1);
+            v[n1] = rem[((16 * n1 + q.j) & (SL - 1)) * N + SL * r + q.c];
+        }
+    }
+    cluster.sync();
+    fft256<false, false>(T, tw, v0, v1);
+    float2* out = dst + (size_t)z * N * N + SL * r;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) out[(size_t)(q.j + 16 * k2) * N + q.c] = v[k2];
+    }
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane_fwd(Args a)
+{
+    extern __shared__ float4 smem4[];
+    float2* smem = reinterpret_cast<float2*>(smem4);
+    float2* tw = smem + (SMEM_COMPLEX - N);
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();
+    const int z = blockIdx.y;
+    load_twiddles(tw, a.tw);
+    float2 v0[16], v1[16];
+    const float2* in = a.src + ((size_t)z * N + SL * r) * N;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) v[n1] = in[(size_t)q.row * N + 16 * n1 + q.j];
+    }
+    __syncthreads();
+    forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
+}
+
+// Inverse y and x FFTs of plane z, the pointwise update, and (FWD) the
+// forward x and y FFTs of the new term.
+template <int EPI, bool FWD>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane_inv(Args a)
+{
+    extern __shared__ float4 smem4[];
+    float2* smem = reinterpret_cast<float2*>(smem4);
+    float2* tw = smem + (SMEM_COMPLEX - N);
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();
+    const int z = blockIdx.y;
+    load_twiddles(tw, a.tw);
+    float2 v0[16], v1[16];
+    // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
+    const float2* in = a.src + (size_t)z * N * N + SL * r;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) v[k2] = in[(size_t)(q.j + 16 * k2) * N + q.c];
+    }
+    __syncthreads();
+    float2* T = smem;
+    fft256<true, false>(T, tw, v0, v1);
+    // columns into this CTA's slice A[y][c]
+    float2* A = smem;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) A[(16 * n1 + q.j) * SL + q.c] = v[n1];
+    }
+    cluster.sync();
+    // rows 32r..: thread (row, j) takes kx = j + 16 k2 from slice k2/2
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+        const int y = SL * r + q.row;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const float2* rem = cluster.map_shared_rank(A, k2 >> 1);
+            v[k2] = rem[y * SL + q.j + 16 * (k2 & 1)];
+        }
+    }
+    cluster.sync();
+    fft256<true, true>(T, tw, v0, v1);
+    // pointwise update on (x = 16 n1 + j, y, z)
+    const EpiArgs& e = a.e;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+        const int y = SL * r + q.row;
+        const size_t rowbase = ((size_t)z * N + y) * N;
+        const float attyz = (EPI == EPI_FIRST) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) {
+            const int x = 16 * n1 + q.j;
+            const size_t i = rowbase + x;
+            const float vsc = __ldg(e.vs + i);
+            const float2 Lx = make_float2(v[n1].x * vsc, v[n1].y * vsc);
+            if (EPI == EPI_SCALE) {
+                e.prev[i] = Lx;
+            } else if (EPI == EPI_FIRST) {
+                const float2 a1 = make_float2(Lx.y, -Lx.x);
+                const float2 w = e.w[i];
+                e.prev[i] = a1;
+                e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+                v[n1] = a1;
+            } else {
+                const float2 am = e.prev[i];
+                const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
+                const float att = __ldg(e.ax + x) * attyz;
+                float2 sm = e.S[i];
+                sm.x = fmaf(e.c1, an.x, sm.x) * att;
+                sm.y = fmaf(e.c1, an.y, sm.y) * att;
+                if (EPI == EPI_MID) {
+                    e.prev[i] = an;
+                    e.S[i] = sm;
+                    v[n1] = an;
+                } else {
+                    e.wout[i] = sm;
+                    if (z == e.gz) {
+                        const int ix = x - e.bl, iy = y - e.bf;
+                        if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
+                            const int c = *e.cur;
+                            if (c >= 0 && c < e.nt) e.gather[(size_t)c * e.nx * e.ny + iy * e.nx + ix] = sm.y;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
+}
+
+// z lines of a 32-wide kx tile at one ky: forward, * |k|, inverse, in place.
+__global__ void __launch_bounds__(THREADS, 2) k_zpass(float2* X, const float2* gtw, const float* kx2,
+                                                      const float* ky2, const float* kz2)
+{
+    extern __shared__ float4 smem4[];
+    float2* smem = reinterpret_cast<float2*>(smem4);
+    float2* tw = smem + (SMEM_COMPLEX - N);
+    load_twiddles(tw, gtw);
+    const int ky = blockIdx.y;
+    const int kx0 = SL * blockIdx.x;
+    float2* base = X + (size_t)ky * N + kx0;
+    const size_t plane = (size_t)N * N;
+    float2 v0[16], v1[16];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + q.j) * plane + q.c];
+    }
+    __syncthreads();
+    fft256<false, false>(smem, tw, v0, v1);
+    const float kyy = __ldg(ky2 + ky);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+        const float kxy = __ldg(kx2 + kx0 + q.c) + kyy;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const float k = sqrtf(kxy + __ldg(kz2 + q.j + 16 * k2));
+            v[k2].x *= k;
+            v[k2].y *= k;
+        }
+    }
+    fft256<true, false>(smem, tw, v0, v1);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + q.j) * plane + q.c] = v[n1];
+    }
+}
+
+}  // namespace plane
+
+bool plane_path_supported(int nxb, int nyb, int nzb)
+{
+    return nxb == plane::N && nyb == plane::N && nzb == plane::N;
+}
+
+cudaError_t configure_plane_kernels()
+{
+    cudaError_t e;
+    const int bytes = (int)plane::SMEM_BYTES;
+#define ALLOW(k)                                                                              \
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != \
+        cudaSuccess)                                                                          \
+        return e
+    ALLOW(plane::k_plane_fwd);
+    ALLOW((plane::k_plane_inv<EPI_FIRST, true>));
+    ALLOW((plane::k_plane_inv<EPI_MID, true>));
+    ALLOW((plane::k_plane_inv<EPI_LAST, false>));
+    ALLOW((plane::k_plane_inv<EPI_MID, false>));
+    ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
+    ALLOW(plane::k_zpass);
+#undef ALLOW
+    return cudaSuccess;
+}
+
+cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const float2* tw)
+{
+    plane::Args a{};
+    a.src = state;
+    a.dst = X;
+    a.tw = tw;
+    plane::k_plane_fwd<<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t)
+{
+    plane::k_zpass<<<dim3(plane::N / plane::SL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(
+        X, tw, t.kx2, t.ky2, t.kz2);
+    return cudaGetLastError();
+}
+
+// mode: EPI_FIRST / EPI_MID with the next forward fused (fwd = true), or
+// EPI_LAST without it.  Xin: spectrum after the z pass; Xout: next spectrum.
+cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float2* Xin, float2* Xout,
+                             const float2* tw, const EpiArgs& e)
+{
+    plane::Args a{};
+    a.src = Xin;
+    a.dst = Xout;
+    a.tw = tw;
+    a.e = e;
+    const dim3 grid(plane::CL, plane::N);
+    if (mode == EPI_FIRST)
+        plane::k_plane_inv<EPI_FIRST, true><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    else if (mode == EPI_MID && fwd)
+        plane::k_plane_inv<EPI_MID, true><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    else if (mode == EPI_MID)
+        plane::k_plane_inv<EPI_MID, false><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    else
+        plane::k_plane_inv<EPI_LAST, false><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    return cudaGetLastError();
+}
+
+// out = v * IFFT3(|k| FFT3(in)) / (R N) with the plane kernels.
+cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
+                                        const float* vs, const float2* tw, const Tables& t)
+{
+    cudaError_t e = launch_plane_fwd(s, in, X, tw);
+    if (e != cudaSuccess) return e;
+    if ((e = launch_zpass(s, X, tw, t)) != cudaSuccess) return e;
+    plane::Args a{};
+    a.src = X;
+    a.tw = tw;
+    a.e.prev = out;
+    a.e.vs = vs;
+    plane::k_plane_inv<EPI_SCALE, false><<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
+    return cudaGetLastError();
+}
+
+int plane_max_active_clusters()
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(plane::CL, plane::N);
+    cfg.blockDim = dim3(plane::THREADS);
+    cfg.dynamicSmemBytes = plane::SMEM_BYTES;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = plane::CL;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (void*)(plane::k_plane_inv<EPI_MID, true>), &cfg) != cudaSuccess)
+        return -1;
+    return n;
+}
+
+}  // namespace ose

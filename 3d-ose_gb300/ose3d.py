@@ -20,6 +20,7 @@ OK = 0
 FIELD_P, FIELD_Q, FIELD_V = 0, 1, 2
 LAYOUT_ZYX, LAYOUT_YXZ = 0, 1
 SPONGE_REFERENCE, SPONGE_CERJAN = 0, 1
+PATH_GENERIC, PATH_PLANE = 0, 1
 
 STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOMEM",
           4: "OSE_ERR_IO", 5: "OSE_ERR_UNSUPPORTED", 6: "OSE_ERR_STATE", 7: "OSE_ERR_NUMERIC"}
@@ -27,7 +28,7 @@ STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOME
 # Every symbol include/ose3d.h declares.
 EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_from_file",
            "ose_destroy", "ose_last_error", "ose_get_derived", "ose_reset_shot", "ose_step",
-           "ose_run", "ose_run_record", "ose_run_timed", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
+           "ose_run", "ose_run_record", "ose_run_timed", "ose_select_path", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
            "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
            "ose_profile_step", "ose_write_outputs", "ose_version"]
 
@@ -100,6 +101,7 @@ def load_library(path: str = LIB_PATH):
         "ose_run": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_run_record": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_run_timed": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_select_path": ([H, ctypes.c_int], ctypes.c_int),
         "ose_get_it": ([H, P(ctypes.c_int)], ctypes.c_int),
         "ose_get_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
         "ose_set_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
@@ -203,6 +205,11 @@ class Modeler:
         ms = ctypes.c_float()
         self._check(self._lib.ose_run_timed(self._h, nsteps, ctypes.byref(ms)))
         return ms.value
+
+    def select_path(self, path: int):
+        """PATH_PLANE (256^3 only) or PATH_GENERIC."""
+        self._check(self._lib.ose_select_path(self._h, path))
+        self._check(self._lib.ose_get_derived(self._h, ctypes.byref(self.derived)))
 
     @property
     def it(self) -> int:

@@ -98,6 +98,8 @@ typedef struct ose_derived {
     int path;                       /* kernel family in use (OSE_PATH_*)     */
 } ose_derived;
 
+/* Kernel families: GENERIC = five-pass FFT operator for any even size up to
+ * 1024 per axis; PLANE = two-pass cluster path for 256^3 padded grids. */
 enum { OSE_PATH_GENERIC = 0, OSE_PATH_PLANE = 1 };
 
 typedef struct ose_handle ose_handle;
@@ -158,6 +160,11 @@ ose_status ose_run_record(ose_handle* h, int nsteps, float* rows_out);
  * stream and copies nothing back.  *ms receives the elapsed device time. */
 ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms);
 
+/* Choose the kernel family: OSE_PATH_PLANE (256^3 padded grids only; the
+ * default there) or OSE_PATH_GENERIC (any size).  Both compute the same
+ * step; the choice exists for comparison and testing. */
+ose_status ose_select_path(ose_handle* h, int path);
+
 /* Steps taken in the current shot. */
 ose_status ose_get_it(const ose_handle* h, int* it);
 
@@ -182,7 +189,7 @@ ose_status ose_get_sponge(const ose_handle* h, float* ax, float* ay, float* az);
 /* Apply the normalised operator once to a packed complex field:
  *   out = v * IFFT3(|k| * FFT3(in)) / (R * nxb*nyb*nzb)
  * in/out are host arrays of nxb*nyb*nzb interleaved (re, im) float pairs,
- * [z][y][x].  This is one application of the operator that
+ * [z][y][x].  Runs on the handle's kernel path.  This is one application of the operator that
  * wavefield_extro_ori2 applies 2(M+1) times per step (ose_3d_lib.cu:668-687:
  * cufftXtExecDescriptorC2C forward, scale_kxkz_3D, inverse, scal_vr_3d); the
  * real and imaginary parts carry two independent real fields. */

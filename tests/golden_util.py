@@ -25,6 +25,8 @@ def model_of(g):
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
+    a = np.asarray(a)
+    b = np.asarray(b)
+    a = a.astype(np.complex128 if np.iscomplexobj(a) else np.float64)
+    b = b.astype(np.complex128 if np.iscomplexobj(b) else np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
