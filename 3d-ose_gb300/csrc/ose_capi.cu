@@ -658,7 +658,7 @@ ose_status ose_apply_operator(ose_handle* h, const float* in, float* out)
 }
 
 ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const char** names,
-                            float* ms, double* bytes, int* launches_per_step)
+                            float* ms, double* bytes, int* launches)
 {
     if (!h || !count || reps < 1) return OSE_ERR_INVALID;
     if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
@@ -677,14 +677,12 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
         h->it += 1;
     }
     *count = nc;
-    int total = 0;
     for (int c = 0; c < nc && c < cap; ++c) {
         if (names) names[c] = kNames[c];
         if (ms) ms[c] = t.count[c] ? t.ms[c] / t.count[c] : 0.f;
         if (bytes) bytes[c] = t.count[c] ? t.bytes[c] / t.count[c] : 0.0;
-        total += t.count[c];
+        if (launches) launches[c] = t.count[c] / reps;
     }
-    if (launches_per_step) *launches_per_step = total / reps;
     return OSE_OK;
 }
 

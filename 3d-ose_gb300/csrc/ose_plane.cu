@@ -269,6 +269,76 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
+// The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
+// recurrence, add_bessel_3d and apply_ABC_Xt of ose_3d_lib.cu:651-870, fused.
+// v holds the unnormalised inverse transform on entry and the new term a_{n+1}
+// (FIRST: a_1) on exit.  Loads are issued 8 cells at a time ahead of any
+// store; the buffers never overlap at different cells, so the restrict
+// qualifiers are exact.
+template <int EPI>
+__device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e, int y, int z, int j)
+{
+    float2* __restrict__ prev = e.prev;
+    float2* __restrict__ S = e.S;
+    float2* __restrict__ wout = e.wout;
+    const float2* __restrict__ w = e.w;
+    const float* __restrict__ vs = e.vs;
+    const size_t rowbase = ((size_t)z * N + y) * N + j;
+    const float attyz = (EPI == EPI_FIRST || EPI == EPI_SCALE) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float vv[8];
+        float2 am[8], sm[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const size_t i = rowbase + 16 * (8 * h + q);
+            vv[q] = __ldg(vs + i);
+            if (EPI == EPI_FIRST) am[q] = w[i];
+            if (EPI == EPI_MID || EPI == EPI_LAST) {
+                am[q] = prev[i];
+                sm[q] = S[i];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int n1 = 8 * h + q;
+            const int x = 16 * n1 + j;
+            const size_t i = rowbase + 16 * n1;
+            const float2 Lx = make_float2(v[n1].x * vv[q], v[n1].y * vv[q]);
+            if (EPI == EPI_SCALE) {
+                prev[i] = Lx;
+            } else if (EPI == EPI_FIRST) {
+                // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1
+                const float2 a1 = make_float2(Lx.y, -Lx.x);
+                prev[i] = a1;
+                S[i] = make_float2(fmaf(e.c0, am[q].x, e.c1 * a1.x), fmaf(e.c0, am[q].y, e.c1 * a1.y));
+                v[n1] = a1;
+            } else {
+                // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att
+                const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
+                const float att = __ldg(e.ax + x) * attyz;
+                float2 s = sm[q];
+                s.x = fmaf(e.c1, an.x, s.x) * att;
+                s.y = fmaf(e.c1, an.y, s.y) * att;
+                if (EPI == EPI_MID) {
+                    prev[i] = an;
+                    S[i] = s;
+                    v[n1] = an;
+                } else {
+                    wout[i] = s;
+                    if (z == e.gz) {
+                        const int ix = x - e.bl, iy = y - e.bf;
+                        if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
+                            const int c = *e.cur;
+                            if (c >= 0 && c < e.nt) e.gather[(size_t)c * e.nx * e.ny + iy * e.nx + ix] = s.y;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
 // Inverse y and x FFTs of plane z, the pointwise update, and (FWD) the
 // forward x and y FFTs of the new term.
 template <int EPI, bool FWD>
@@ -319,52 +389,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     cluster.sync();
     fft256<true, true>(T, tw, v0, v1);
     // pointwise update on (x = 16 n1 + j, y, z)
-    const EpiArgs& e = a.e;
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const RowSlot q = row_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-        const int y = SL * r + q.row;
-        const size_t rowbase = ((size_t)z * N + y) * N;
-        const float attyz = (EPI == EPI_FIRST) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
-#pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) {
-            const int x = 16 * n1 + q.j;
-            const size_t i = rowbase + x;
-            const float vsc = __ldg(e.vs + i);
-            const float2 Lx = make_float2(v[n1].x * vsc, v[n1].y * vsc);
-            if (EPI == EPI_SCALE) {
-                e.prev[i] = Lx;
-            } else if (EPI == EPI_FIRST) {
-                const float2 a1 = make_float2(Lx.y, -Lx.x);
-                const float2 w = e.w[i];
-                e.prev[i] = a1;
-                e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
-                v[n1] = a1;
-            } else {
-                const float2 am = e.prev[i];
-                const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
-                const float att = __ldg(e.ax + x) * attyz;
-                float2 sm = e.S[i];
-                sm.x = fmaf(e.c1, an.x, sm.x) * att;
-                sm.y = fmaf(e.c1, an.y, sm.y) * att;
-                if (EPI == EPI_MID) {
-                    e.prev[i] = an;
-                    e.S[i] = sm;
-                    v[n1] = an;
-                } else {
-                    e.wout[i] = sm;
-                    if (z == e.gz) {
-                        const int ix = x - e.bl, iy = y - e.bf;
-                        if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
-                            const int c = *e.cur;
-                            if (c >= 0 && c < e.nt) e.gather[(size_t)c * e.nx * e.ny + iy * e.nx + ix] = sm.y;
-                        }
-                    }
-                }
-            }
-        }
-    }
+    epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
+    epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
     if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 

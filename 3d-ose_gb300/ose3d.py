@@ -260,13 +260,13 @@ class Modeler:
         names = (ctypes.c_char_p * cap)()
         ms = np.zeros(cap, np.float32)
         by = np.zeros(cap, np.float64)
-        lps = ctypes.c_int()
+        launches = (ctypes.c_int * cap)()
         self._check(self._lib.ose_profile_step(self._h, reps, cap, ctypes.byref(count), names,
                                                _f32(ms), by.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                               ctypes.byref(lps)))
-        rows = [dict(name=names[i].decode(), ms=float(ms[i]), bytes=float(by[i]))
-                for i in range(count.value)]
-        return rows, lps.value
+                                               launches))
+        rows = [dict(name=names[i].decode(), ms=float(ms[i]), bytes=float(by[i]),
+                     launches_per_step=int(launches[i])) for i in range(count.value)]
+        return rows, sum(r["launches_per_step"] for r in rows)
 
     def write_outputs(self, gather_path: str | None, par_path: str | None):
         self._check(self._lib.ose_write_outputs(

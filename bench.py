@@ -224,7 +224,7 @@ def main():
 
     # per-kernel launch durations (events bracketing each launch, one step)
     rows, launches_per_step = m.profile_step(reps=2)
-    per_step = {r["name"]: (d.M + 1 if r["name"] != "inject" else 1) for r in rows}
+    per_step = {r["name"]: r["launches_per_step"] for r in rows}
     share = {r["name"]: r["ms"] * per_step[r["name"]] for r in rows}
     total = sum(share.values())
     dom = max(rows, key=lambda r: share[r["name"]])

@@ -195,13 +195,15 @@ ose_status ose_get_sponge(const ose_handle* h, float* ax, float* ay, float* az);
  * real and imaginary parts carry two independent real fields. */
 ose_status ose_apply_operator(ose_handle* h, const float* in, float* out);
 
-/* Average device time per launch of each kernel class over one step, measured
- * with CUDA events bracketing each launch on the handle's stream (not graph
- * replay).  names/ms/bytes are arrays of capacity cap; *count receives the
- * number of classes.  bytes = algorithmic HBM bytes of one launch. */
+/* Average device time per launch of each kernel class over `reps` steps,
+ * measured with CUDA events bracketing each launch on the handle's stream
+ * (not graph replay).  Advances the shot by `reps` steps.  names, ms, bytes
+ * and launches are arrays of capacity cap; *count receives the number of
+ * classes.  bytes = algorithmic HBM bytes of one launch; launches = launches
+ * of the class per step. */
 ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count,
                             const char** names, float* ms, double* bytes,
-                            int* launches_per_step);
+                            int* launches);
 
 /* Write ./output-style files of the current shot:
  * gather [ig][it] (ose_3d.cu:276) to gather_path and the parameter dump
