@@ -207,6 +207,13 @@ __device__ __forceinline__ void load_twiddles(float2* tw, const float2* g)
     for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = g[t];
 }
 
+// Bulk prefetch of a contiguous range into L2 (no registers, no shared
+// memory); p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Forward x FFT of this CTA's 32 rows (values in v0/v1, spatial order) then
 // forward y FFT of its 32 columns; spectrum stored to dst plane z.
 __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* smem, const float2* tw,
@@ -350,6 +357,18 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
+    // The epilogue's operands of this CTA's 32 rows are contiguous: start
+    // pulling them into L2 now, so the epilogue's loads hit L2.
+    if (threadIdx.x == 0 && EPI != EPI_SCALE) {
+        const size_t row0 = ((size_t)z * N + SL * r) * N;
+        prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
+        if (EPI == EPI_FIRST) {
+            prefetch_l2(a.e.w + row0, SL * N * sizeof(float2));
+        } else {
+            prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
+            prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
+        }
+    }
     load_twiddles(tw, a.tw);
     float2 v0[16], v1[16];
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
@@ -392,6 +411,62 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
     epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
     if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
+}
+
+// z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
+// One line slot per thread (column c = t % 16, line thread j = t / 16) keeps
+// registers near 64 so four CTAs share an SM.
+constexpr int ZW = 16;
+constexpr size_t ZSMEM_BYTES = sizeof(float2) * (16 * 16 * ZW + N);
+
+__global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
+                                                        const float* __restrict__ kx2,
+                                                        const float* __restrict__ ky2,
+                                                        const float* __restrict__ kz2)
+{
+    extern __shared__ float4 smem4[];
+    float2* T = reinterpret_cast<float2*>(smem4);
+    float2* tw = T + 16 * 16 * ZW;
+    load_twiddles(tw, gtw);
+    const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
+    const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
+    float2* base = X + (size_t)ky * N + kx;
+    const size_t plane = (size_t)N * N;
+    float2 v[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + j) * plane];
+    __syncthreads();
+    // forward: DFT16 over n1, twiddle, transpose, DFT16 over n2
+    dft16<false>(v);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) v[k] = cmul(v[k], tw[j * k]);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
+    __syncthreads();
+    dft16<false>(v);
+    // v[k2] = spectrum at kz = j + 16 k2
+    const float kxy = __ldg(kx2 + kx) + __ldg(ky2 + ky);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+        const float k = sqrtf(kxy + __ldg(kz2 + j + 16 * k2));
+        v[k2].x *= k;
+        v[k2].y *= k;
+    }
+    // inverse: IDFT16 over k2, twiddle, transpose, IDFT16 over k1
+    dft16<true>(v);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) v[k] = cmulc(v[k], tw[j * k]);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
+    dft16<true>(v);
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + j) * plane] = v[n1];
 }
 
 // z lines of a 32-wide kx tile at one ky: forward, * |k|, inverse, in place.
@@ -461,6 +536,7 @@ cudaError_t configure_plane_kernels()
     ALLOW((plane::k_plane_inv<EPI_MID, false>));
     ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
     ALLOW(plane::k_zpass);
+    ALLOW(plane::k_zpass16);
 #undef ALLOW
     return cudaSuccess;
 }
@@ -477,7 +553,7 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
 
 cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t)
 {
-    plane::k_zpass<<<dim3(plane::N / plane::SL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(
+    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::THREADS, plane::ZSMEM_BYTES, s>>>(
         X, tw, t.kx2, t.ky2, t.kz2);
     return cudaGetLastError();
 }
