@@ -129,16 +129,17 @@ __device__ float2* fft_lines(float2* a, float2* b, int L, int LS, int ES, bool l
     return a;
 }
 
-enum { EPI_NONE = -1 };
+// EPI_SCALE_VEL: out = X * vel[i] * c0 (velocity and 1/(R N) given separately).
+enum { EPI_NONE = -1, EPI_SCALE_VEL = 4 };
 
 // The pointwise work of one application on cell i = (x, y, z); X is the
 // unnormalised inverse transform.
 template <int EPI>
 __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float2 X, const EpiArgs& e)
 {
-    const float v = __ldg(e.vs + i);
+    const float v = EPI == EPI_SCALE_VEL ? __ldg(e.vs + i) * e.c0 : __ldg(e.vs + i);
     const float2 Lx = cscale(X, v);
-    if (EPI == EPI_SCALE) {
+    if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
         e.prev[i] = Lx;
     } else if (EPI == EPI_FIRST) {
         // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1   (ose_3d_lib.cu:651-744)
@@ -404,6 +405,27 @@ cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float*
                           const float* hil, int* ctr, int nt)
 {
     k_inject<<<1, 1, 0, s>>>(W, src, ricker, hil, ctr, nt);
+    return cudaGetLastError();
+}
+
+// The generic operator with the velocity and 1/(R N) given separately, for
+// callers that hold a plain velocity array: out = vel * scale * IFFT3(|k| FFT3(in)).
+// X is caller-provided scratch of one field.
+cudaError_t launch_apply_operator_vel(cudaStream_t s, const Geometry& g, const AxisPlan& px,
+                                      const AxisPlan& py, const AxisPlan& pz, const Tables& t,
+                                      const float2* in, float2* X, float2* out, const float* vel,
+                                      float scale)
+{
+    cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, in, X, nullptr);
+    if (err != cudaSuccess) return err;
+    EpiArgs e{};
+    e.prev = out;
+    e.vs = vel;
+    e.c0 = scale;
+    const long long nrows = (long long)g.nyb * g.nzb;
+    const int rpc = rows_per_cta(px.n);
+    k_rows<true, EPI_SCALE_VEL><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
+        X, nullptr, g, px, t.twx, rpc, e);
     return cudaGetLastError();
 }
 

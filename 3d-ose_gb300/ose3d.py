@@ -21,6 +21,7 @@ FIELD_P, FIELD_Q, FIELD_V = 0, 1, 2
 LAYOUT_ZYX, LAYOUT_YXZ = 0, 1
 SPONGE_REFERENCE, SPONGE_CERJAN = 0, 1
 PATH_GENERIC, PATH_PLANE = 0, 1
+NOALLOC_MAX_CELLS = 262144   # OSE_NOALLOC_MAX_CELLS
 
 STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOMEM",
           4: "OSE_ERR_IO", 5: "OSE_ERR_UNSUPPORTED", 6: "OSE_ERR_STATE", 7: "OSE_ERR_NUMERIC"}
@@ -30,7 +31,7 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_destroy", "ose_last_error", "ose_get_derived", "ose_reset_shot", "ose_step",
            "ose_run", "ose_run_record", "ose_run_timed", "ose_select_path", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
            "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
-           "ose_profile_step", "ose_write_outputs", "ose_version"]
+           "ose_profile_step", "ose_write_outputs", "ose_version", "ose_apply_operator_noalloc"]
 
 
 class OseError(RuntimeError):
@@ -113,6 +114,9 @@ def load_library(path: str = LIB_PATH):
                               f32, P(ctypes.c_double), P(ctypes.c_int)], ctypes.c_int),
         "ose_write_outputs": ([H, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
         "ose_version": ([], ctypes.c_char_p),
+        "ose_apply_operator_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -120,6 +124,16 @@ def load_library(path: str = LIB_PATH):
         fn.restype = res
     _lib = L
     return L
+
+
+def apply_operator_noalloc(nxb: int, nyb: int, nzb: int, dx: float, dy: float, dz: float, R: float,
+                           vel_ptr: int, in_ptr: int, out_ptr: int, stream: int = 0) -> int:
+    """ose_apply_operator_noalloc on device pointers (integers, e.g. from a
+    framework tensor's data pointer); returns the ose_status.  For callers that
+    cannot allocate device memory: the library allocates nothing here."""
+    return load_library().ose_apply_operator_noalloc(
+        nxb, nyb, nzb, dx, dy, dz, R, ctypes.c_void_p(vel_ptr), ctypes.c_void_p(in_ptr),
+        ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream) if stream else None)
 
 
 def default_params(**kw) -> Params:

@@ -205,6 +205,32 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count,
                             const char** names, float* ms, double* bytes,
                             int* launches);
 
+/* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
+#define OSE_NOALLOC_MAX_CELLS 262144
+
+/* The operator of ose_apply_operator on caller-owned DEVICE buffers, with no
+ * allocation of any kind.  This entry point has no counterpart in the
+ * reference; it exists for callers that cannot call cudaMalloc: code running
+ * inside a framework that owns the device allocator (a plugin or custom call
+ * that must not allocate behind it), hosts that must not allocate after
+ * start-up, and callers that already own every buffer.
+ *   out = vel * IFFT3(|k| FFT3(in)) / (R * nxb*nyb*nzb)
+ * vel: nxb*nyb*nzb floats (padded velocity, [z][y][x]); in, out: as many
+ * interleaved (re, im) float pairs; all three in device memory, out may not
+ * alias in.  |k| uses dk = 2 pi / (d * nb) per axis.  stream: a cudaStream_t
+ * (NULL = the legacy default stream); the call only enqueues work.
+ * Limits: nxb*nyb*nzb <= OSE_NOALLOC_MAX_CELLS, every axis even and at most
+ * 1024; larger sizes return OSE_ERR_UNSUPPORTED.  The FFT scratch and the
+ * twiddle/wavenumber tables live in one fixed device array of about 2 MiB
+ * that every GPU loading the library keeps until the process exits; every
+ * call shares it and leaves its contents behind, so calls that overlap on
+ * the GPU (several streams or host threads) race: serialise them.  The first
+ * call on a device looks up that array's address and sets kernel attributes;
+ * make it before any stream capture. */
+ose_status ose_apply_operator_noalloc(int nxb, int nyb, int nzb, float dx, float dy, float dz,
+                                      double R, const float* vel, const float* in, float* out,
+                                      void* stream);
+
 /* Write ./output-style files of the current shot:
  * gather [ig][it] (ose_3d.cu:276) to gather_path and the parameter dump
  * (output_par, ose_3d_lib.cu:255-319) to par_path.  Either may be NULL. */
