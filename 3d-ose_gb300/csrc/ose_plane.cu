@@ -199,7 +199,6 @@ struct Args {
     const float* kx2;
     const float* ky2;
     const float* kz2;
-    int lookahead;         // planes per wave of co-resident clusters
     EpiArgs e;
 };
 
@@ -255,25 +254,6 @@ __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* s
     }
 }
 
-// Pull plane z's inputs of this CTA into L2: the 256 rows of its spectrum
-// column slab (256 B each, one per thread) and/or, for the pointwise update,
-// its 32 contiguous rows of the operands.
-template <int EPI>
-__device__ __forceinline__ void prefetch_plane(const Args& a, int z, int r, bool spectrum, bool operands)
-{
-    if (spectrum) prefetch_l2(a.src + (size_t)z * N * N + (size_t)threadIdx.x * N + SL * r, SL * sizeof(float2));
-    if (operands && threadIdx.x == 0 && EPI != EPI_SCALE) {
-        const size_t row0 = ((size_t)z * N + SL * r) * N;
-        prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
-        if (EPI == EPI_FIRST) {
-            prefetch_l2(a.e.w + row0, SL * N * sizeof(float2));
-        } else {
-            prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
-            prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
-        }
-    }
-}
-
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane_fwd(Args a)
 {
     extern __shared__ float4 smem4[];
@@ -296,12 +276,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
-constexpr int EPI_CHUNK = 4;   // cells of a slot whose operands are loaded together
-
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
 // recurrence, add_bessel_3d and apply_ABC_Xt of ose_3d_lib.cu:651-870, fused.
 // v holds the unnormalised inverse transform on entry and the new term a_{n+1}
-// (FIRST: a_1) on exit.  Loads are issued EPI_CHUNK cells at a time ahead of any
+// (FIRST: a_1) on exit.  Loads are issued 8 cells at a time ahead of any
 // store; the buffers never overlap at different cells, so the restrict
 // qualifiers are exact.
 template <int EPI>
@@ -315,12 +293,12 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
     const size_t rowbase = ((size_t)z * N + y) * N + j;
     const float attyz = (EPI == EPI_FIRST || EPI == EPI_SCALE) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
 #pragma unroll
-    for (int h = 0; h < 16 / EPI_CHUNK; ++h) {
-        float vv[EPI_CHUNK];
-        float2 am[EPI_CHUNK], sm[EPI_CHUNK];
+    for (int h = 0; h < 2; ++h) {
+        float vv[8];
+        float2 am[8], sm[8];
 #pragma unroll
-        for (int q = 0; q < EPI_CHUNK; ++q) {
-            const size_t i = rowbase + 16 * (EPI_CHUNK * h + q);
+        for (int q = 0; q < 8; ++q) {
+            const size_t i = rowbase + 16 * (8 * h + q);
             vv[q] = __ldg(vs + i);
             if (EPI == EPI_FIRST) am[q] = w[i];
             if (EPI == EPI_MID || EPI == EPI_LAST) {
@@ -329,8 +307,8 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
             }
         }
 #pragma unroll
-        for (int q = 0; q < EPI_CHUNK; ++q) {
-            const int n1 = EPI_CHUNK * h + q;
+        for (int q = 0; q < 8; ++q) {
+            const int n1 = 8 * h + q;
             const int x = 16 * n1 + j;
             const size_t i = rowbase + 16 * n1;
             const float2 Lx = make_float2(v[n1].x * vv[q], v[n1].y * vv[q]);
@@ -378,58 +356,61 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     float2* tw = smem + (SMEM_COMPLEX - N);
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
-    load_twiddles(tw, a.tw);
-    // Pull this plane's epilogue operands into L2 now, and the inputs of the
-    // plane one wave of co-resident clusters ahead, which a later cluster
-    // will start on when this wave drains.
     const int z = blockIdx.y;
-    prefetch_plane<EPI>(a, z, r, false, true);
-    if (z + a.lookahead < N) prefetch_plane<EPI>(a, z + a.lookahead, r, true, false);
-    {
-        float2 v0[16], v1[16];
-        // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
-        const float2* in = a.src + (size_t)z * N * N + SL * r;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const ColSlot q = col_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-            for (int k2 = 0; k2 < 16; ++k2) v[k2] = in[(size_t)(q.j + 16 * k2) * N + q.c];
+    // The epilogue's operands of this CTA's 32 rows are contiguous: start
+    // pulling them into L2 now, so the epilogue's loads hit L2.
+    if (threadIdx.x == 0 && EPI != EPI_SCALE) {
+        const size_t row0 = ((size_t)z * N + SL * r) * N;
+        prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
+        if (EPI == EPI_FIRST) {
+            prefetch_l2(a.e.w + row0, SL * N * sizeof(float2));
+        } else {
+            prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
+            prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
         }
-        __syncthreads();
-        float2* T = smem;
-        fft256<true, false>(T, tw, v0, v1);
-        // columns into this CTA's slice A[y][c]
-        float2* A = smem;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const ColSlot q = col_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-            for (int n1 = 0; n1 < 16; ++n1) A[(16 * n1 + q.j) * SL + q.c] = v[n1];
-        }
-        cluster.sync();
-        // rows 32r..: thread (row, j) takes kx = j + 16 k2 from slice k2/2
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const RowSlot q = row_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-            const int y = SL * r + q.row;
-#pragma unroll
-            for (int k2 = 0; k2 < 16; ++k2) {
-                const float2* rem = cluster.map_shared_rank(A, k2 >> 1);
-                v[k2] = rem[y * SL + q.j + 16 * (k2 & 1)];
-            }
-        }
-        // after this barrier no CTA reads another's slice again in this
-        // plane, so the slice may be reused as exchange space
-        cluster.sync();
-        fft256<true, true>(T, tw, v0, v1);
-        // pointwise update on (x = 16 n1 + j, y, z)
-        epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
-        epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
-        if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
     }
+    load_twiddles(tw, a.tw);
+    float2 v0[16], v1[16];
+    // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
+    const float2* in = a.src + (size_t)z * N * N + SL * r;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) v[k2] = in[(size_t)(q.j + 16 * k2) * N + q.c];
+    }
+    __syncthreads();
+    float2* T = smem;
+    fft256<true, false>(T, tw, v0, v1);
+    // columns into this CTA's slice A[y][c]
+    float2* A = smem;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) A[(16 * n1 + q.j) * SL + q.c] = v[n1];
+    }
+    cluster.sync();
+    // rows 32r..: thread (row, j) takes kx = j + 16 k2 from slice k2/2
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+        const int y = SL * r + q.row;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const float2* rem = cluster.map_shared_rank(A, k2 >> 1);
+            v[k2] = rem[y * SL + q.j + 16 * (k2 & 1)];
+        }
+    }
+    cluster.sync();
+    fft256<true, true>(T, tw, v0, v1);
+    // pointwise update on (x = 16 n1 + j, y, z)
+    epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
+    epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
+    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
 // z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
@@ -441,61 +422,51 @@ constexpr size_t ZSMEM_BYTES = sizeof(float2) * (16 * 16 * ZW + N);
 __global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
                                                         const float* __restrict__ kx2,
                                                         const float* __restrict__ ky2,
-                                                        const float* __restrict__ kz2, int lookahead)
+                                                        const float* __restrict__ kz2)
 {
     extern __shared__ float4 smem4[];
     float2* T = reinterpret_cast<float2*>(smem4);
     float2* tw = T + 16 * 16 * ZW;
     load_twiddles(tw, gtw);
     const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
+    const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
+    float2* base = X + (size_t)ky * N + kx;
     const size_t plane = (size_t)N * N;
-    constexpr int kTiles = (N / ZW) * N;   // (kx tile, ky) pairs
-    // Thread t pulls z row t of the tile one wave of co-resident CTAs ahead
-    // into L2, for the CTA that will start on it when this wave drains.
-    const int tile = blockIdx.x;
-    const int nxt = tile + lookahead;
-    if (nxt < kTiles)
-        prefetch_l2(X + (size_t)threadIdx.x * plane + (nxt / (N / ZW)) * N + ZW * (nxt % (N / ZW)),
-                    ZW * sizeof(float2));
-    {
-        const int ky = tile / (N / ZW), kx = ZW * (tile % (N / ZW)) + c;
-        float2* base = X + (size_t)ky * N + kx;
-        float2 v[16];
+    float2 v[16];
 #pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + j) * plane];
-        __syncthreads();   // twiddles loaded
-        // forward: DFT16 over n1, twiddle, transpose, DFT16 over n2
-        dft16<false>(v);
+    for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + j) * plane];
+    __syncthreads();
+    // forward: DFT16 over n1, twiddle, transpose, DFT16 over n2
+    dft16<false>(v);
 #pragma unroll
-        for (int k = 1; k < 16; ++k) v[k] = cmul(v[k], tw[j * k]);
+    for (int k = 1; k < 16; ++k) v[k] = cmul(v[k], tw[j * k]);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
-        __syncthreads();
+    for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
+    __syncthreads();
 #pragma unroll
-        for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
-        __syncthreads();
-        dft16<false>(v);
-        // v[k2] = spectrum at kz = j + 16 k2
-        const float kxy = __ldg(kx2 + kx) + __ldg(ky2 + ky);
+    for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
+    __syncthreads();
+    dft16<false>(v);
+    // v[k2] = spectrum at kz = j + 16 k2
+    const float kxy = __ldg(kx2 + kx) + __ldg(ky2 + ky);
 #pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2) {
-            const float k = sqrtf(kxy + __ldg(kz2 + j + 16 * k2));
-            v[k2].x *= k;
-            v[k2].y *= k;
-        }
-        // inverse: IDFT16 over k2, twiddle, transpose, IDFT16 over k1
-        dft16<true>(v);
-#pragma unroll
-        for (int k = 1; k < 16; ++k) v[k] = cmulc(v[k], tw[j * k]);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
-        __syncthreads();
-#pragma unroll
-        for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
-        dft16<true>(v);
-#pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + j) * plane] = v[n1];
+    for (int k2 = 0; k2 < 16; ++k2) {
+        const float k = sqrtf(kxy + __ldg(kz2 + j + 16 * k2));
+        v[k2].x *= k;
+        v[k2].y *= k;
     }
+    // inverse: IDFT16 over k2, twiddle, transpose, IDFT16 over k1
+    dft16<true>(v);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) v[k] = cmulc(v[k], tw[j * k]);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
+    dft16<true>(v);
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + j) * plane] = v[n1];
 }
 
 // z lines of a 32-wide kx tile at one ky: forward, * |k|, inverse, in place.
@@ -550,13 +521,6 @@ bool plane_path_supported(int nxb, int nyb, int nzb)
     return nxb == plane::N && nyb == plane::N && nzb == plane::N;
 }
 
-namespace {
-// Prefetch distances, set by configure_plane_kernels: co-resident 8-CTA
-// clusters of the plane kernels, co-resident CTAs of the z pass.
-int g_plane_clusters = plane::N;
-int g_zpass_ctas = (plane::N / plane::ZW) * plane::N;
-}  // namespace
-
 cudaError_t configure_plane_kernels()
 {
     cudaError_t e;
@@ -574,16 +538,6 @@ cudaError_t configure_plane_kernels()
     ALLOW(plane::k_zpass);
     ALLOW(plane::k_zpass16);
 #undef ALLOW
-    const int nc = plane_max_active_clusters();
-    g_plane_clusters = nc > 0 ? (nc < plane::N ? nc : plane::N) : plane::N;
-    int dev = 0, sms = 0, per_sm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plane::k_zpass16, plane::THREADS,
-                                                           plane::ZSMEM_BYTES)) != cudaSuccess)
-        return e;
-    const int tiles = (plane::N / plane::ZW) * plane::N;
-    g_zpass_ctas = per_sm > 0 ? (sms * per_sm < tiles ? sms * per_sm : tiles) : tiles;
     return cudaSuccess;
 }
 
@@ -599,8 +553,8 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
 
 cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t)
 {
-    plane::k_zpass16<<<(plane::N / plane::ZW) * plane::N, plane::THREADS, plane::ZSMEM_BYTES, s>>>(
-        X, tw, t.kx2, t.ky2, t.kz2, g_zpass_ctas);
+    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::THREADS, plane::ZSMEM_BYTES, s>>>(
+        X, tw, t.kx2, t.ky2, t.kz2);
     return cudaGetLastError();
 }
 
@@ -614,7 +568,6 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     a.dst = Xout;
     a.tw = tw;
     a.e = e;
-    a.lookahead = g_plane_clusters;
     const dim3 grid(plane::CL, plane::N);
     if (mode == EPI_FIRST)
         plane::k_plane_inv<EPI_FIRST, true><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
@@ -639,7 +592,6 @@ cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2
     a.tw = tw;
     a.e.prev = out;
     a.e.vs = vs;
-    a.lookahead = g_plane_clusters;
     plane::k_plane_inv<EPI_SCALE, false><<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
     return cudaGetLastError();
 }
