@@ -1,0 +1,71 @@
+"""Long-run accuracy of the FP32 GPU path against the FP64 restatement
+(oracle/oracle_torch.py, run with torch on the same GPU) on a bench workload.
+
+    python tests/accuracy_long.py [--workload ose256] [--steps 2000] [--every 250]
+
+Prints one JSON line per checkpoint: step, rel-L2 of the gather so far and of
+the current P and Q, plus the first dropped series coefficient |J_{M+2}(dtR)|.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+for sub in ("", "oracle", "3d-ose_gb300"):
+    sys.path.insert(0, os.path.join(ROOT, sub))
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="ose256")
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--every", type=int, default=250)
+    ap.add_argument("--path", default="default", choices=["default", "generic"])
+    a = ap.parse_args()
+    import __graft_entry__ as ge
+    ge.build_library()
+    import ose3d
+    import workloads
+    from oracle_torch import TorchOracle
+
+    build, kw = workloads.CONFIGS[a.workload]
+    vel = build()
+    steps = min(a.steps, kw["nt"])
+    m = ose3d.Modeler(ose3d.default_params(**kw), vel)
+    if a.path == "generic":
+        m.select_path(ose3d.PATH_GENERIC)
+    m.reset_shot(0)
+    t = TorchOracle(kw, vel, "cuda")
+    rows32, rows64 = [], []
+    done = 0
+    t0 = time.time()
+    while done < steps:
+        n = min(a.every, steps - done)
+        rows32.append(m.run_record(n))
+        rows64.append(t.run(n))
+        done += n
+        g32, g64 = np.concatenate(rows32), np.concatenate(rows64)
+        out = {"workload": a.workload, "path": "plane" if m.derived.path == 1 else "generic",
+               "step": done, "gather_rel_l2": rel(g32, g64),
+               "P_rel_l2": rel(m.wavefield(ose3d.FIELD_P), t.P()),
+               "Q_rel_l2": rel(m.wavefield(ose3d.FIELD_Q), t.Q()),
+               "M": m.derived.M, "bessel_tail": m.derived.bessel_tail,
+               "elapsed_s": round(time.time() - t0, 1)}
+        print(json.dumps(out), flush=True)
+    m.close()
+
+
+if __name__ == "__main__":
+    main()

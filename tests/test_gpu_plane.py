@@ -91,3 +91,21 @@ def test_plane_graph_replay_matches_steps(model):
         m.reset_shot(0)
         m.run(3)
         assert np.array_equal(q_steps, m.wavefield(ose3d.FIELD_Q))
+
+
+def test_plane_path_matches_fp64_over_200_steps(model):
+    """FP32 plane path vs the FP64 restatement (torch, same GPU) after 200
+    steps of the 256^3 workload: gather and final wavefield within 1e-4."""
+    torch = pytest.importorskip("torch")
+    from oracle_torch import TorchOracle
+    with ose3d.Modeler(ose3d.default_params(**KW), model) as m:
+        m.reset_shot(0)
+        g32 = m.run_record(200)
+        P, Q = m.wavefield(ose3d.FIELD_P), m.wavefield(ose3d.FIELD_Q)
+    t = TorchOracle(KW, model, "cuda")
+    g64 = t.run(200)
+    assert rel_l2(g32, g64) < 1e-4
+    assert rel_l2(Q, t.Q()) < 1e-4
+    assert rel_l2(P, t.P()) < 1e-4
+    del t
+    torch.cuda.empty_cache()
