@@ -2,6 +2,7 @@
 // device memory, the step sequence and its CUDA-graph replay.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -11,6 +12,7 @@
 #include <vector>
 
 #include "ose_internal.h"
+#include "ose_io.h"
 
 using ose::AxisPlan;
 
@@ -50,6 +52,14 @@ struct ose_handle {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     ose::KernelTiming timing{};
+
+    // snapshots (allocated on first use): device copy of the state, two
+    // pinned host buffers, a copy stream and its events
+    float2* Wsnap = nullptr;
+    float2* hsnap[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_ready = nullptr;
+    cudaEvent_t snap_done[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -100,6 +110,13 @@ void free_all(ose_handle* h)
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->timing.ev[0]) cudaEventDestroy(h->timing.ev[0]);
     if (h->timing.ev[1]) cudaEventDestroy(h->timing.ev[1]);
+    if (h->Wsnap) cudaFree(h->Wsnap);
+    for (int b = 0; b < 2; ++b) {
+        if (h->hsnap[b]) cudaFreeHost(h->hsnap[b]);
+        if (h->snap_done[b]) cudaEventDestroy(h->snap_done[b]);
+    }
+    if (h->snap_ready) cudaEventDestroy(h->snap_ready);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -457,9 +474,9 @@ ose_status ose_destroy(ose_handle* h)
     return OSE_OK;
 }
 
-ose_status ose_reset_shot(ose_handle* h, int is)
+// Source cell and source traces of shot `is` (no change to the wavefield).
+static ose_status prepare_shot(ose_handle* h, int is)
 {
-    if (!h) return OSE_ERR_INVALID;
     const ose_params& p = h->p;
     if (is < 0) return fail(h, OSE_ERR_INVALID, "negative shot index");
     // source: sg_init_host then the decode of Xt_add_wavelet_sxyz (ose_3d_lib.cu:598-616)
@@ -476,16 +493,25 @@ ose_status ose_reset_shot(ose_handle* h, int is)
     // Alloc_wavelet (ose_3d_lib.cu:557-586)
     ose::ricker_trace(p.nt, p.fm, p.dt, p.amp, h->h_ricker);
     ose::hilbert_trace(h->h_ricker, p.hilbert_div_nt, h->h_hil);
-    const size_t N = (size_t)h->g.ncell;
     CK(h, upload(h, h->ricker, h->h_ricker));
     CK(h, upload(h, h->hil, h->h_hil));
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }   // src may have moved
+    h->shot = is;
+    return OSE_OK;
+}
+
+ose_status ose_reset_shot(ose_handle* h, int is)
+{
+    if (!h) return OSE_ERR_INVALID;
+    ose_status st = prepare_shot(h, is);
+    if (st != OSE_OK) return st;
+    const ose_params& p = h->p;
+    const size_t N = (size_t)h->g.ncell;
     // Xtdata_value: the state starts at rest
     CK(h, cudaMemsetAsync(h->W, 0, sizeof(float2) * N, h->stream));
     CK(h, cudaMemsetAsync(h->gather, 0, sizeof(float) * (size_t)p.nt * h->d.ng, h->stream));
     CK(h, cudaMemsetAsync(h->ctr, 0, sizeof(int) * 4, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }   // src may have moved
-    h->shot = is;
     h->it = 0;
     h->shot_ready = true;
     return OSE_OK;
@@ -740,5 +766,169 @@ ose_status ose_write_outputs(ose_handle* h, const char* gather_path, const char*
     }
     return OSE_OK;
 }
+
+/* ---- checkpoint / resume ------------------------------------------------- */
+
+namespace {
+const char kCkMagic[8] = {'O', 'S', 'E', '3', 'D', 'C', 'K', '1'};
+struct CkHeader {
+    char magic[8];
+    int32_t version, params_bytes;
+    int32_t nxb, nyb, nzb, nt, ng, shot, it;
+};
+}  // namespace
+
+ose_status ose_checkpoint_save(ose_handle* h, const char* path)
+{
+    if (!h || !path) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    const size_t N = (size_t)h->g.ncell;
+    std::vector<float2> w(N);
+    std::vector<float> g((size_t)h->it * h->d.ng);
+    CK(h, cudaMemcpyAsync(w.data(), h->W, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
+    if (!g.empty())
+        CK(h, cudaMemcpyAsync(g.data(), h->gather, sizeof(float) * g.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    CkHeader hd;
+    memcpy(hd.magic, kCkMagic, 8);
+    hd.version = 1;
+    hd.params_bytes = (int32_t)sizeof(ose_params);
+    hd.nxb = h->d.nxb; hd.nyb = h->d.nyb; hd.nzb = h->d.nzb;
+    hd.nt = h->p.nt; hd.ng = h->d.ng; hd.shot = h->shot; hd.it = h->it;
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(h, OSE_ERR_IO, std::string("cannot write ") + path);
+    bool ok = fwrite(&hd, sizeof hd, 1, f) == 1 && fwrite(&h->p, sizeof(ose_params), 1, f) == 1 &&
+              fwrite(w.data(), sizeof(float2), N, f) == N &&
+              (g.empty() || fwrite(g.data(), sizeof(float), g.size(), f) == g.size());
+    if (fclose(f) != 0) ok = false;
+    return ok ? OSE_OK : fail(h, OSE_ERR_IO, std::string("short write ") + path);
+}
+
+ose_status ose_checkpoint_load(ose_handle* h, const char* path)
+{
+    if (!h || !path) return OSE_ERR_INVALID;
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(h, OSE_ERR_IO, std::string("cannot open ") + path);
+    CkHeader hd;
+    ose_params p;
+    bool ok = fread(&hd, sizeof hd, 1, f) == 1;
+    if (!ok || memcmp(hd.magic, kCkMagic, 8) != 0 || hd.version != 1 || hd.params_bytes != (int32_t)sizeof(ose_params)) {
+        fclose(f);
+        return fail(h, OSE_ERR_IO, std::string("not an ose3d checkpoint: ") + path);
+    }
+    ok = fread(&p, sizeof p, 1, f) == 1;
+    if (!ok || memcmp(&p, &h->p, sizeof p) != 0 || hd.nxb != h->d.nxb || hd.nyb != h->d.nyb ||
+        hd.nzb != h->d.nzb || hd.it < 0 || hd.it > h->p.nt) {
+        fclose(f);
+        return fail(h, OSE_ERR_INVALID, "checkpoint was written with other parameters");
+    }
+    const size_t N = (size_t)h->g.ncell;
+    std::vector<float2> w(N);
+    std::vector<float> g((size_t)hd.it * h->d.ng);
+    ok = fread(w.data(), sizeof(float2), N, f) == N &&
+         (g.empty() || fread(g.data(), sizeof(float), g.size(), f) == g.size());
+    fclose(f);
+    if (!ok) return fail(h, OSE_ERR_IO, std::string("truncated checkpoint ") + path);
+    ose_status st = prepare_shot(h, hd.shot);
+    if (st != OSE_OK) return st;
+    CK(h, cudaMemcpyAsync(h->W, w.data(), sizeof(float2) * N, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemsetAsync(h->gather, 0, sizeof(float) * (size_t)h->p.nt * h->d.ng, h->stream));
+    if (!g.empty())
+        CK(h, cudaMemcpyAsync(h->gather, g.data(), sizeof(float) * g.size(), cudaMemcpyHostToDevice, h->stream));
+    int ctr[4] = {hd.it, hd.it > 0 ? hd.it - 1 : 0, 0, 0};
+    CK(h, cudaMemcpyAsync(h->ctr, ctr, sizeof ctr, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->it = hd.it;
+    h->shot_ready = true;
+    return OSE_OK;
+}
+
+/* ---- snapshots ------------------------------------------------------------ */
+
+ose_status ose_run_snapshots(ose_handle* h, int nsteps, int every, int layout, ose_snapshot_fn fn, void* user)
+{
+    if (!h || !fn || every < 1 || nsteps < 0) return OSE_ERR_INVALID;
+    if (layout != OSE_LAYOUT_ZYX && layout != OSE_LAYOUT_YXZ) return fail(h, OSE_ERR_INVALID, "bad layout");
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    if (h->it + nsteps > h->p.nt) return fail(h, OSE_ERR_INVALID, "nsteps beyond nt");
+    const size_t N = (size_t)h->g.ncell;
+    if (!h->Wsnap) {
+        CK(h, dalloc(h, &h->Wsnap, N));
+        for (int b = 0; b < 2; ++b) {
+            CK(h, cudaMallocHost((void**)&h->hsnap[b], sizeof(float2) * N));
+            CK(h, cudaEventCreateWithFlags(&h->snap_done[b], cudaEventDisableTiming));
+        }
+        CK(h, cudaEventCreateWithFlags(&h->snap_ready, cudaEventDisableTiming));
+        CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    }
+    ose_status st = build_graph(h);
+    if (st != OSE_OK) return st;
+    const int K = (nsteps + every - 1) / every;
+    std::vector<int> its(K);
+    std::vector<float> P(N), Q(N), tmp(N);
+    // batch k: its steps, then W -> Wsnap (device) and Wsnap -> hsnap[k % 2] on
+    // the copy stream; the host hands snapshot k to fn while batch k+1 runs.
+    auto enqueue = [&](int k) -> ose_status {
+        const int n = std::min(every, nsteps - k * every);
+        for (int i = 0; i < n; ++i) CK(h, cudaGraphLaunch(h->graph, h->stream));
+        h->it += n;
+        its[k] = h->it - 1;
+        if (k > 0) CK(h, cudaStreamWaitEvent(h->stream, h->snap_done[(k - 1) % 2], 0));
+        CK(h, cudaMemcpyAsync(h->Wsnap, h->W, sizeof(float2) * N, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, cudaEventRecord(h->snap_ready, h->stream));
+        CK(h, cudaStreamWaitEvent(h->copy_stream, h->snap_ready, 0));
+        CK(h, cudaMemcpyAsync(h->hsnap[k % 2], h->Wsnap, sizeof(float2) * N, cudaMemcpyDeviceToHost,
+                              h->copy_stream));
+        CK(h, cudaEventRecord(h->snap_done[k % 2], h->copy_stream));
+        return OSE_OK;
+    };
+    if (K > 0 && (st = enqueue(0)) != OSE_OK) return st;
+    for (int k = 0; k < K; ++k) {
+        if (k + 1 < K && (st = enqueue(k + 1)) != OSE_OK) return st;
+        CK(h, cudaEventSynchronize(h->snap_done[k % 2]));
+        const float2* w = h->hsnap[k % 2];
+        for (size_t i = 0; i < N; ++i) { P[i] = w[i].x; Q[i] = w[i].y; }
+        if (layout == OSE_LAYOUT_YXZ) {
+            to_layout(h, P.data(), tmp.data(), layout);
+            P.swap(tmp);
+            to_layout(h, Q.data(), tmp.data(), layout);
+            Q.swap(tmp);
+        }
+        fn(its[k], P.data(), Q.data(), user);
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return OSE_OK;
+}
+
+/* ---- SU / SEG-Y ------------------------------------------------------------ */
+
+static ose_status write_traces(ose_handle* h, const char* path, bool segy)
+{
+    if (!h || !path) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    const ose_params& p = h->p;
+    std::vector<float> g((size_t)p.nt * h->d.ng);
+    ose_status st = ose_get_gather(h, g.data());
+    if (st != OSE_OK) return st;
+    ose::TraceGeometry tg{};
+    tg.ng = h->d.ng;
+    tg.nt = p.nt;
+    tg.nx = p.nx;
+    tg.shot = h->shot;
+    tg.dx = p.dx;
+    tg.dy = p.dy;
+    tg.sx = (double)(p.sxbeg + h->shot * p.jsx) * p.dx;
+    tg.sy = (double)(p.sybeg + h->shot * p.jsy) * p.dy;
+    tg.sz = (double)(p.szbeg + h->shot * p.jsz) * p.dz;
+    tg.gz = (double)p.gzbeg * p.dz;
+    tg.dt_us = (int)lround((double)p.dt * 1e6);
+    const int rc = ose::write_gather_traces(path, g.data(), tg, segy);
+    if (rc == -2) return fail(h, OSE_ERR_UNSUPPORTED, "nt or dt does not fit the 16-bit trace header fields");
+    if (rc != 0) return fail(h, OSE_ERR_IO, std::string("cannot write ") + path);
+    return OSE_OK;
+}
+
+ose_status ose_write_su(ose_handle* h, const char* path) { return write_traces(h, path, false); }
+ose_status ose_write_segy(ose_handle* h, const char* path) { return write_traces(h, path, true); }
 
 }  // extern "C"

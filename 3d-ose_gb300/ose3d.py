@@ -31,7 +31,13 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_destroy", "ose_last_error", "ose_get_derived", "ose_reset_shot", "ose_step",
            "ose_run", "ose_run_record", "ose_run_timed", "ose_select_path", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
            "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
-           "ose_profile_step", "ose_write_outputs", "ose_version", "ose_apply_operator_noalloc"]
+           "ose_profile_step", "ose_write_outputs", "ose_version", "ose_apply_operator_noalloc",
+           "ose_checkpoint_save", "ose_checkpoint_load", "ose_run_snapshots", "ose_write_su",
+           "ose_write_segy"]
+
+# void (*)(int it, const float* P, const float* Q, void* user)
+SNAPSHOT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                               ctypes.POINTER(ctypes.c_float), ctypes.c_void_p)
 
 
 class OseError(RuntimeError):
@@ -114,6 +120,12 @@ def load_library(path: str = LIB_PATH):
                               f32, P(ctypes.c_double), P(ctypes.c_int)], ctypes.c_int),
         "ose_write_outputs": ([H, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
         "ose_version": ([], ctypes.c_char_p),
+        "ose_checkpoint_save": ([H, ctypes.c_char_p], ctypes.c_int),
+        "ose_checkpoint_load": ([H, ctypes.c_char_p], ctypes.c_int),
+        "ose_run_snapshots": ([H, ctypes.c_int, ctypes.c_int, ctypes.c_int, SNAPSHOT_FN, ctypes.c_void_p],
+                              ctypes.c_int),
+        "ose_write_su": ([H, ctypes.c_char_p], ctypes.c_int),
+        "ose_write_segy": ([H, ctypes.c_char_p], ctypes.c_int),
         "ose_apply_operator_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                         ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -281,6 +293,39 @@ class Modeler:
         rows = [dict(name=names[i].decode(), ms=float(ms[i]), bytes=float(by[i]),
                      launches_per_step=int(launches[i])) for i in range(count.value)]
         return rows, sum(r["launches_per_step"] for r in rows)
+
+    def checkpoint_save(self, path: str):
+        self._check(self._lib.ose_checkpoint_save(self._h, path.encode()))
+
+    def checkpoint_load(self, path: str):
+        self._check(self._lib.ose_checkpoint_load(self._h, path.encode()))
+
+    def run_snapshots(self, nsteps: int, every: int, callback, layout: int = LAYOUT_ZYX):
+        """nsteps steps; callback(it, P, Q) after every `every` steps with numpy
+        copies of the padded P and Q (shape of `layout`)."""
+        d = self.derived
+        shape = self.shape if layout == LAYOUT_ZYX else (d.nyb, d.nxb, d.nzb)
+        n = d.nxb * d.nyb * d.nzb
+        errors = []
+
+        def tramp(it, p, q, _user):
+            try:
+                P = np.ctypeslib.as_array(p, shape=(n,)).copy().reshape(shape)
+                Q = np.ctypeslib.as_array(q, shape=(n,)).copy().reshape(shape)
+                callback(it, P, Q)
+            except Exception as exc:   # keep going; report after the run
+                errors.append(exc)
+
+        fn = SNAPSHOT_FN(tramp)
+        self._check(self._lib.ose_run_snapshots(self._h, nsteps, every, layout, fn, None))
+        if errors:
+            raise errors[0]
+
+    def write_su(self, path: str):
+        self._check(self._lib.ose_write_su(self._h, path.encode()))
+
+    def write_segy(self, path: str):
+        self._check(self._lib.ose_write_segy(self._h, path.encode()))
 
     def write_outputs(self, gather_path: str | None, par_path: str | None):
         self._check(self._lib.ose_write_outputs(

@@ -205,6 +205,39 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count,
                             const char** names, float* ms, double* bytes,
                             int* launches);
 
+/* Checkpoint of the current shot to a file: parameters, shot index, step
+ * index, P and Q, and the receiver rows recorded so far - the whole state of
+ * the time loop.  The reference has no checkpoint; its state is exactly these
+ * (the p2D/q2D fields, it, rec_data_h: ose_3d.cu:242-276). */
+ose_status ose_checkpoint_save(ose_handle* h, const char* path);
+
+/* Restore a checkpoint on a handle created with identical parameters; the
+ * shot then continues from the saved step (ose_run, ose_step...). */
+ose_status ose_checkpoint_load(ose_handle* h, const char* path);
+
+/* Called by ose_run_snapshots with the 0-based index of the last step done
+ * and the padded P and Q (nxb*nyb*nzb floats each, in the requested layout).
+ * The arrays are valid during the call only. */
+typedef void (*ose_snapshot_fn)(int it, const float* P, const float* Q, void* user);
+
+/* nsteps steps; after every `every` steps (and after the last) the state is
+ * copied out and handed to fn.  Copies go device -> device -> pinned host on a
+ * second stream while the next steps run, so the callback overlaps the GPU
+ * work.  With OSE_LAYOUT_YXZ the arrays have the byte layout of the
+ * reference's commented per-step dump ./wf/{p,q}-<it>-single.bin
+ * (ose_3d.cu:260-269, write_3dfile_from_1darray_ci). */
+ose_status ose_run_snapshots(ose_handle* h, int nsteps, int every, int layout,
+                             ose_snapshot_fn fn, void* user);
+
+/* The current shot's gather (ng traces x nt samples, trace ig = iy*nx + ix)
+ * as an SU file (240-byte SEG-Y trace headers, native byte order, no file
+ * header) or as a SEG-Y file (3200-byte text + 400-byte binary header,
+ * big-endian IEEE float traces).  Coordinates in cm (scalco = -100), dt in
+ * microseconds.  The reference names SU formats (ose_3d.cu:17-18) but writes
+ * only raw floats. */
+ose_status ose_write_su(ose_handle* h, const char* path);
+ose_status ose_write_segy(ose_handle* h, const char* path);
+
 /* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
 #define OSE_NOALLOC_MAX_CELLS 262144
 

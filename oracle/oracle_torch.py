@@ -17,10 +17,15 @@ import oracle as O
 
 
 class TorchOracle:
-    def __init__(self, params: dict, vel_xyz: np.ndarray, device: str = "cpu", shot: int = 0):
+    def __init__(self, params: dict, vel_xyz: np.ndarray, device: str = "cpu", shot: int = 0,
+                 single: bool = False):
+        """single=True runs the same loop in complex64 / float32 (the
+        arithmetic class of the reference's cuFFT FP32 path), for comparison."""
         import torch
 
         self.torch = torch
+        self.rdt = torch.float32 if single else torch.float64
+        self.cdt = torch.complex64 if single else torch.complex128
         self.dev = torch.device(device)
         p = O.make_params(**params)
         d = O.derive(p)
@@ -34,7 +39,7 @@ class TorchOracle:
         az = O.sponge(p.bu, p.nz, d.bd, p.sponge_mode, p.cerjan_factor).astype(np.float64)
         self.ricker = O.ricker(p.nt, p.fm, p.dt, p.amp).astype(np.float64)
         self.hil = O.hilbert(self.ricker.astype(np.float32), bool(p.hilbert_div_nt)).astype(np.float64)
-        t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=self.dev)  # noqa: E731
+        t = lambda a: torch.as_tensor(a, dtype=self.rdt, device=self.dev)  # noqa: E731
         self.att = t(az[:, None, None] * ay[None, :, None] * ax[None, None, :])
         # v / R; torch's inverse FFT already divides by N (ose_3d_kernel.cu:355-357)
         self.vr = t(vb.astype(np.float64) / self.R)
@@ -50,7 +55,7 @@ class TorchOracle:
         sxyz = sz0 * nx * ny + sy0 * nx + sx0
         self.src = (p.bu + sxyz // (nx * ny), p.bf + sxyz % (nx * ny) // nx, p.bl + sxyz % (nx * ny) % nx)
         self.gz = p.bu + p.gzbeg
-        self.W = torch.zeros(self.shape, dtype=torch.complex128, device=self.dev)
+        self.W = torch.zeros(self.shape, dtype=self.cdt, device=self.dev)
         self.it = 0
 
     def L(self, x):
@@ -77,10 +82,10 @@ class TorchOracle:
     def run(self, nsteps: int):
         """Gather rows [it][ig] of the next nsteps steps (float64 numpy)."""
         rows = [self.step() for _ in range(nsteps)]
-        return self.torch.stack(rows).cpu().numpy()
+        return self.torch.stack(rows).cpu().numpy().astype(np.float64)
 
     def P(self):
-        return self.W.real.cpu().numpy()
+        return self.W.real.cpu().numpy().astype(np.float64)
 
     def Q(self):
-        return self.W.imag.cpu().numpy()
+        return self.W.imag.cpu().numpy().astype(np.float64)

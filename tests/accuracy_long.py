@@ -32,7 +32,7 @@ def main():
     ap.add_argument("--workload", default="ose256")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--every", type=int, default=250)
-    ap.add_argument("--path", default="default", choices=["default", "generic"])
+    ap.add_argument("--path", default="default", choices=["default", "generic", "torch32"])
     a = ap.parse_args()
     import __graft_entry__ as ge
     ge.build_library()
@@ -43,28 +43,35 @@ def main():
     build, kw = workloads.CONFIGS[a.workload]
     vel = build()
     steps = min(a.steps, kw["nt"])
-    m = ose3d.Modeler(ose3d.default_params(**kw), vel)
+    # torch32: the same loop in complex64 with cuFFT, the arithmetic class of
+    # the reference's FP32 cuFFT path, in place of libose3d
+    m = None if a.path == "torch32" else ose3d.Modeler(ose3d.default_params(**kw), vel)
     if a.path == "generic":
         m.select_path(ose3d.PATH_GENERIC)
-    m.reset_shot(0)
+    if m is not None:
+        m.reset_shot(0)
+    t32 = TorchOracle(kw, vel, "cuda", single=True) if m is None else None
     t = TorchOracle(kw, vel, "cuda")
     rows32, rows64 = [], []
     done = 0
     t0 = time.time()
     while done < steps:
         n = min(a.every, steps - done)
-        rows32.append(m.run_record(n))
+        rows32.append(m.run_record(n) if m is not None else t32.run(n))
         rows64.append(t.run(n))
         done += n
         g32, g64 = np.concatenate(rows32), np.concatenate(rows64)
-        out = {"workload": a.workload, "path": "plane" if m.derived.path == 1 else "generic",
-               "step": done, "gather_rel_l2": rel(g32, g64),
-               "P_rel_l2": rel(m.wavefield(ose3d.FIELD_P), t.P()),
-               "Q_rel_l2": rel(m.wavefield(ose3d.FIELD_Q), t.Q()),
-               "M": m.derived.M, "bessel_tail": m.derived.bessel_tail,
-               "elapsed_s": round(time.time() - t0, 1)}
+        P32 = m.wavefield(ose3d.FIELD_P) if m is not None else t32.P()
+        Q32 = m.wavefield(ose3d.FIELD_Q) if m is not None else t32.Q()
+        P64, Q64 = t.P(), t.Q()
+        name = "torch32" if m is None else ("plane" if m.derived.path == 1 else "generic")
+        out = {"workload": a.workload, "path": name, "step": done,
+               "gather_rel_l2": rel(g32, g64), "P_rel_l2": rel(P32, P64), "Q_rel_l2": rel(Q32, Q64),
+               "Q_norm": float(np.linalg.norm(Q64)), "P_norm": float(np.linalg.norm(P64)),
+               "M": t.M, "elapsed_s": round(time.time() - t0, 1)}
         print(json.dumps(out), flush=True)
-    m.close()
+    if m is not None:
+        m.close()
 
 
 if __name__ == "__main__":
