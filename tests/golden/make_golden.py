@@ -100,6 +100,9 @@ def run_case(case, ref_dir):
             att_x=rd("temp/att_x_0.bin")[:nxb], att_y=rd("temp/att_y.bin"), att_z=rd("temp/att_z.bin"),
             ricker=rd("temp/ricker_card.bin"), hilbert=rd("temp/hilbert_card.bin"),
             ricker_hil_main=rd("temp/ricker_hil.bin"),
+            att_x_dump=rd("temp/att_x_0.bin"),
+            partest=np.array(open(os.path.join(td, "output/partest.txt"), "rb").read()),
+            qshot2_bytes=np.int64(os.path.getsize(os.path.join(td, "output/qshot2.bin"))),
             gather=gather,
             vmax=np.float32(float(stats["vmax"])), M=np.int32(int(stats["M"])),
             dims=np.array([nxb, nyb, nzb], np.int32),
