@@ -32,7 +32,8 @@ def main():
     ap.add_argument("--workload", default="ose256")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--every", type=int, default=250)
-    ap.add_argument("--path", default="default", choices=["default", "generic", "torch32"])
+    ap.add_argument("--path", default="default",
+                    choices=["default", "generic", "torch32", "fp64c32"])
     a = ap.parse_args()
     import __graft_entry__ as ge
     ge.build_library()
@@ -45,12 +46,17 @@ def main():
     steps = min(a.steps, kw["nt"])
     # torch32: the same loop in complex64 with cuFFT, the arithmetic class of
     # the reference's FP32 cuFFT path, in place of libose3d
-    m = None if a.path == "torch32" else ose3d.Modeler(ose3d.default_params(**kw), vel)
+    # fp64c32: FP64 arithmetic with the per-step constants rounded to float32
+    m = None if a.path in ("torch32", "fp64c32") else ose3d.Modeler(ose3d.default_params(**kw), vel)
     if a.path == "generic":
         m.select_path(ose3d.PATH_GENERIC)
     if m is not None:
         m.reset_shot(0)
-    t32 = TorchOracle(kw, vel, "cuda", single=True) if m is None else None
+    t32 = None
+    if a.path == "torch32":
+        t32 = TorchOracle(kw, vel, "cuda", single=True)
+    elif a.path == "fp64c32":
+        t32 = TorchOracle(kw, vel, "cuda", fp32_constants=True)
     t = TorchOracle(kw, vel, "cuda")
     rows32, rows64 = [], []
     done = 0
@@ -64,7 +70,7 @@ def main():
         P32 = m.wavefield(ose3d.FIELD_P) if m is not None else t32.P()
         Q32 = m.wavefield(ose3d.FIELD_Q) if m is not None else t32.Q()
         P64, Q64 = t.P(), t.Q()
-        name = "torch32" if m is None else ("plane" if m.derived.path == 1 else "generic")
+        name = a.path if m is None else ("plane" if m.derived.path == 1 else "generic")
         out = {"workload": a.workload, "path": name, "step": done,
                "gather_rel_l2": rel(g32, g64), "P_rel_l2": rel(P32, P64), "Q_rel_l2": rel(Q32, Q64),
                "Q_norm": float(np.linalg.norm(Q64)), "P_norm": float(np.linalg.norm(P64)),
