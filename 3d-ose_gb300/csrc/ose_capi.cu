@@ -32,9 +32,12 @@ struct ose_handle {
     float2* A = nullptr;     // a_odd
     float2* S = nullptr;     // partial sum
     float2* X = nullptr;     // FFT scratch
-    float* vs = nullptr;     // v / (R N)
+    float* vs = nullptr;     // velocity v per cell (padded model)
     float *ax = nullptr, *ay = nullptr, *az = nullptr;
     float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
+    float *kx2l = nullptr, *ky2l = nullptr, *kz2l = nullptr;   // low parts
+    float2* twxl = nullptr;                                     // low parts of W_nxb
+    float sch = 0.f, scl = 0.f;                                 // 1 / (R N) as hi + lo
     float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
     float *ricker = nullptr, *hil = nullptr;
     float* gather = nullptr; // [nt][ng]
@@ -103,7 +106,8 @@ void free_all(ose_handle* h)
 {
     if (h->graph) cudaGraphExecDestroy(h->graph);
     void* bufs[] = {h->W, h->A, h->S, h->X, h->vs, h->ax, h->ay, h->az, h->kx2, h->ky2, h->kz2,
-                    h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr};
+                    h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr,
+                    h->kx2l, h->ky2l, h->kz2l, h->twxl};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -153,6 +157,8 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
     const int M = h->d.M;
     ose::EpiArgs ea{};
     ea.vs = h->vs;
+    ea.sch = h->sch;
+    ea.scl = h->scl;
     ea.ax = h->ax;
     ea.ay = h->ay;
     ea.az = h->az;
@@ -166,10 +172,10 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
     ea.nx = h->p.nx;
     ea.ny = h->p.ny;
     ea.nt = h->p.nt;
-    e = timed(tm, s, 0, 16.0 * N, [&] { return ose::launch_plane_fwd(s, h->W, h->X, h->twx); });
+    e = timed(tm, s, 0, 16.0 * N, [&] { return ose::launch_plane_fwd(s, h->W, h->X, h->tables); });
     if (e != cudaSuccess) return e;
     for (int n = 0; n <= M; ++n) {
-        e = timed(tm, s, 1, 16.0 * N, [&] { return ose::launch_zpass(s, h->X, h->twx, h->tables); });
+        e = timed(tm, s, 1, 16.0 * N, [&] { return ose::launch_zpass(s, h->X, h->tables); });
         if (e != cudaSuccess) return e;
         ose::EpiMode mode;
         double bytes;
@@ -177,20 +183,20 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
         if (n == 0) {
             ea.prev = h->A;
             ea.w = h->W;
-            ea.c0 = (float)h->J[0];
-            ea.c1 = (float)(2.0 * h->J[1]);
+            ose::split_float(h->J[0], &ea.c0, &ea.c0l);
+            ose::split_float(2.0 * h->J[1], &ea.c1, &ea.c1l);
             mode = ose::EPI_FIRST;
             bytes = (M > 0 ? 44.0 : 36.0) * N;
             cls = 2;
         } else {
             ea.prev = (n & 1) ? h->W : h->A;
-            ea.c1 = (float)(2.0 * h->J[n + 1]);
+            ose::split_float(2.0 * h->J[n + 1], &ea.c1, &ea.c1l);
             mode = n == M ? ose::EPI_LAST : ose::EPI_MID;
             bytes = (n == M ? 36.0 : 52.0) * N;
             cls = n == M ? 4 : 3;
         }
         const bool fwd = n < M;
-        e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->twx, ea); });
+        e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->tables, ea); });
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -208,6 +214,8 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
     const int M = h->d.M;
     ose::EpiArgs ea{};
     ea.vs = h->vs;
+    ea.sch = h->sch;
+    ea.scl = h->scl;
     ea.ax = h->ax;
     ea.ay = h->ay;
     ea.az = h->az;
@@ -225,8 +233,8 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
     // n = 0: a_1 = -i L a_0, S = J0 a_0 + 2 J1 a_1
     ea.prev = h->A;
     ea.w = h->W;
-    ea.c0 = (float)h->J[0];
-    ea.c1 = (float)(2.0 * h->J[1]);
+    ose::split_float(h->J[0], &ea.c0, &ea.c0l);
+    ose::split_float(2.0 * h->J[1], &ea.c1, &ea.c1l);
     e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->W, h->X,
                                         ose::EPI_FIRST, ea, tm);
     if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += 36.0 * N; }
@@ -234,7 +242,7 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
     for (int n = 1; n <= M; ++n) {
         const float2* an = (n & 1) ? h->A : h->W;
         ea.prev = (n & 1) ? h->W : h->A;
-        ea.c1 = (float)(2.0 * h->J[n + 1]);
+        ose::split_float(2.0 * h->J[n + 1], &ea.c1, &ea.c1l);
         e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, an, h->X,
                                             n == M ? ose::EPI_LAST : ose::EPI_MID, ea, tm);
         if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += (n == M ? 36.0 : 44.0) * N; }
@@ -375,16 +383,17 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     ose::sponge_table(p.bl, p.nx, d.br, p.sponge_mode, p.cerjan_factor, h->h_ax);
     ose::sponge_table(p.bf, p.ny, d.bb, p.sponge_mode, p.cerjan_factor, h->h_ay);
     ose::sponge_table(p.bu, p.nz, d.bd, p.sponge_mode, p.cerjan_factor, h->h_az);
-    std::vector<float> kx2, ky2, kz2, vs(N);
-    ose::k2_table(d.nxb, d.dkx, kx2);
-    ose::k2_table(d.nyb, d.dky, ky2);
-    ose::k2_table(d.nzb, d.dkz, kz2);
-    std::vector<float2> twx, twy, twz;
-    ose::twiddle_table(d.nxb, twx);
+    std::vector<float> kx2, ky2, kz2, kx2l, ky2l, kz2l;
+    ose::k2_table(d.nxb, d.dkx, kx2, &kx2l);
+    ose::k2_table(d.nyb, d.dky, ky2, &ky2l);
+    ose::k2_table(d.nzb, d.dkz, kz2, &kz2l);
+    std::vector<float2> twx, twy, twz, twxl;
+    ose::twiddle_table(d.nxb, twx, &twxl);
     ose::twiddle_table(d.nyb, twy);
     ose::twiddle_table(d.nzb, twz);
-    const double sc = 1.0 / (d.R * (double)N);
-    for (size_t i = 0; i < N; ++i) vs[i] = (float)((double)h->vb[i] * sc);
+    // L = v * IFFT3(|k| FFT3(.)) * (1 / (R N)): the device keeps v itself and
+    // applies 1/(R N) as a float pair
+    ose::split_float(1.0 / (d.R * (double)N), &h->sch, &h->scl);
 
     cudaError_t e = cudaGetDevice(&h->device);
     if (e != cudaSuccess) { ose_status s = cuda_fail(nullptr, e, "cudaGetDevice"); delete h; return s; }
@@ -420,11 +429,19 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(dalloc(h, &h->twx, d.nxb));
     CKC(dalloc(h, &h->twy, d.nyb));
     CKC(dalloc(h, &h->twz, d.nzb));
+    CKC(dalloc(h, &h->twxl, d.nxb));
+    CKC(dalloc(h, &h->kx2l, d.nxb));
+    CKC(dalloc(h, &h->ky2l, d.nyb));
+    CKC(dalloc(h, &h->kz2l, d.nzb));
     CKC(dalloc(h, &h->ricker, (size_t)p.nt));
     CKC(dalloc(h, &h->hil, (size_t)p.nt));
     CKC(dalloc(h, &h->gather, (size_t)p.nt * d.ng));
     CKC(dalloc(h, &h->ctr, 4));
-    CKC(upload(h, h->vs, vs));
+    CKC(upload(h, h->vs, h->vb));
+    CKC(upload(h, h->twxl, twxl));
+    CKC(upload(h, h->kx2l, kx2l));
+    CKC(upload(h, h->ky2l, ky2l));
+    CKC(upload(h, h->kz2l, kz2l));
     CKC(upload(h, h->ax, h->h_ax));
     CKC(upload(h, h->ay, h->h_ay));
     CKC(upload(h, h->az, h->h_az));
@@ -444,6 +461,10 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     h->tables.kx2 = h->kx2;
     h->tables.ky2 = h->ky2;
     h->tables.kz2 = h->kz2;
+    h->tables.twl = h->twxl;
+    h->tables.kx2l = h->kx2l;
+    h->tables.ky2l = h->ky2l;
+    h->tables.kz2l = h->kz2l;
     d.path = ose::plane_path_supported(d.nxb, d.nyb, d.nzb) ? OSE_PATH_PLANE : OSE_PATH_GENERIC;
     if (const char* env = getenv("OSE3D_PATH"))
         if (!strcmp(env, "generic")) d.path = OSE_PATH_GENERIC;
@@ -675,9 +696,10 @@ ose_status ose_apply_operator(ose_handle* h, const float* in, float* out)
     // A and S carry no state between steps, so they serve as in/out here.
     CK(h, cudaMemcpyAsync(h->A, in, sizeof(float2) * N, cudaMemcpyHostToDevice, h->stream));
     if (h->d.path == OSE_PATH_PLANE)
-        CK(h, ose::launch_plane_apply_operator(h->stream, h->A, h->X, h->S, h->vs, h->twx, h->tables));
+        CK(h, ose::launch_plane_apply_operator(h->stream, h->A, h->X, h->S, h->vs, h->sch, h->scl, h->tables));
     else
-        CK(h, ose::launch_apply_operator(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->A, h->X, h->S, h->vs));
+        CK(h, ose::launch_apply_operator(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->A, h->X, h->S, h->vs,
+                                         h->sch, h->scl));
     CK(h, cudaMemcpyAsync(out, h->S, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return OSE_OK;

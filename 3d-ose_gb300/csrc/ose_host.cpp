@@ -162,23 +162,35 @@ int plan_axis(int n, AxisPlan* p)
     return 0;
 }
 
-// W_n^t = exp(-2 pi i t / n), t < n, rounded from double.
-void twiddle_table(int n, std::vector<float2>& out)
+// W_n^t = exp(-2 pi i t / n), t < n: nearest floats, and (if lo) the
+// remainders, so hi + lo carries the twiddle to about 48 bits.
+void twiddle_table(int n, std::vector<float2>& out, std::vector<float2>* lo)
 {
     out.resize(n);
+    if (lo) lo->resize(n);
     for (int t = 0; t < n; ++t) {
-        double a = -2.0 * M_PI * (double)t / n;
-        out[t] = make_float2((float)cos(a), (float)sin(a));
+        const double a = -2.0 * M_PI * (double)t / n;
+        const double c = cos(a), s = sin(a);
+        float ch, cl, sh, sl;
+        split_float(c, &ch, &cl);
+        split_float(s, &sh, &sl);
+        out[t] = make_float2(ch, sh);
+        if (lo) (*lo)[t] = make_float2(cl, sl);
     }
 }
 
-// (dk * wrapped index)^2 as scale_kxkz_3D wraps it (ose_3d_kernel.cu:109-120).
-void k2_table(int n, double dk, std::vector<float>& out)
+// (dk * wrapped index)^2 as scale_kxkz_3D wraps it (ose_3d_kernel.cu:109-120),
+// nearest floats and (if lo) the remainders.
+void k2_table(int n, double dk, std::vector<float>& out, std::vector<float>* lo)
 {
     out.resize(n);
+    if (lo) lo->resize(n);
     for (int i = 0; i < n; ++i) {
-        double k = dk * (i > n / 2 ? n - i : i);
-        out[i] = (float)(k * k);
+        const double k = dk * (i > n / 2 ? n - i : i);
+        float h, l;
+        split_float(k * k, &h, &l);
+        out[i] = h;
+        if (lo) (*lo)[i] = l;
     }
 }
 

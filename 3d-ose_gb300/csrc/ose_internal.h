@@ -36,11 +36,15 @@ struct EpiArgs {
     const float2* w;      // FIRST: a_0 = W
     float2* S;            // partial sum
     float2* wout;         // LAST: new state (P, Q)
-    const float* vs;      // v / (R N), per cell
+    const float* vs;      // velocity v per cell (the model value itself)
     const float* ax;      // sponge, x
     const float* ay;      // sponge, y
     const float* az;      // sponge, z
-    float c0, c1;         // FIRST: J0, 2 J1.  MID/LAST: c1 = 2 J_{n+1}
+    // Constants as unevaluated float pairs hi + lo (about 48 significant
+    // bits), so that no rounded constant biases every step the same way:
+    float c0, c0l;        // FIRST: J0
+    float c1, c1l;        // FIRST: 2 J1.  MID/LAST: 2 J_{n+1}
+    float sch, scl;       // 1 / (R N), the scale of v * IFFT3(|k| FFT3(.))
     // receivers (LAST)
     float* gather;        // [nt][ng]
     const int* cur;       // current step index
@@ -54,7 +58,18 @@ struct Tables {
     const float* kx2;     // squared wrapped wavenumbers
     const float* ky2;
     const float* kz2;
+    const float2* twl;    // plane path: low parts of W_256^t (twx = high parts)
+    const float* kx2l;    // plane path: low parts of the squared wavenumbers
+    const float* ky2l;
+    const float* kz2l;
 };
+
+// hi + lo split of a double: hi = nearest float, lo = nearest float to the rest.
+inline void split_float(double v, float* hi, float* lo)
+{
+    *hi = (float)v;
+    *lo = (float)(v - (double)*hi);
+}
 
 // Host-side launch helpers (ose_kernels.cu).
 struct KernelTiming;
@@ -66,18 +81,19 @@ cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float*
                           const float* hil, int* ctr, int nt);
 cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                   const AxisPlan& py, const AxisPlan& pz, const Tables& t,
-                                  const float2* in, float2* X, float2* out, const float* vs);
+                                  const float2* in, float2* X, float2* out, const float* vs,
+                                  float sch, float scl);
 cudaError_t configure_kernels();
 
 // 256^3 fast path (ose_plane.cu).
 bool plane_path_supported(int nxb, int nyb, int nzb);
 cudaError_t configure_plane_kernels();
-cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const float2* tw);
-cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t);
+cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const Tables& t);
+cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t);
 cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float2* Xin, float2* Xout,
-                             const float2* tw, const EpiArgs& e);
+                             const Tables& t, const EpiArgs& e);
 cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
-                                        const float* vs, const float2* tw, const Tables& t);
+                                        const float* vs, float sch, float scl, const Tables& t);
 int plane_max_active_clusters();
 
 // Per-kernel-class timing used by ose_profile_step.
@@ -97,8 +113,8 @@ void pad_model(const ose_params& p, const ose_derived& d, const float* vel_xyz, 
 void sponge_table(int before, int nn, int after, int mode, float factor, std::vector<float>& out);
 void ricker_trace(int nt, float fm, float dt, float amp, std::vector<float>& out);
 void hilbert_trace(const std::vector<float>& w, int div_nt, std::vector<float>& out);
-void twiddle_table(int n, std::vector<float2>& out);
-void k2_table(int n, double dk, std::vector<float>& out);
+void twiddle_table(int n, std::vector<float2>& out, std::vector<float2>* lo = nullptr);
+void k2_table(int n, double dk, std::vector<float>& out, std::vector<float>* lo = nullptr);
 int derive_dims(const ose_params& p, ose_derived* d, std::string* err);
 void series_params(const ose_params& p, float vmax, ose_derived* d);
 

@@ -129,16 +129,17 @@ __device__ float2* fft_lines(float2* a, float2* b, int L, int LS, int ES, bool l
     return a;
 }
 
-// EPI_SCALE_VEL: out = X * vel[i] * c0 (velocity and 1/(R N) given separately).
+// EPI_SCALE_VEL: out = X * vel[i] * scale (the allocation-free entry point)
 enum { EPI_NONE = -1, EPI_SCALE_VEL = 4 };
 
 // The pointwise work of one application on cell i = (x, y, z); X is the
-// unnormalised inverse transform.
+// unnormalised inverse transform, e.vs the velocity, (e.sch + e.scl) = 1/(R N).
 template <int EPI>
 __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float2 X, const EpiArgs& e)
 {
-    const float v = EPI == EPI_SCALE_VEL ? __ldg(e.vs + i) * e.c0 : __ldg(e.vs + i);
-    const float2 Lx = cscale(X, v);
+    const float v = __ldg(e.vs + i);
+    float2 Lx = cscale(X, v);
+    Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
     if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
         e.prev[i] = Lx;
     } else if (EPI == EPI_FIRST) {
@@ -146,15 +147,16 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
         const float2 a1 = make_float2(Lx.y, -Lx.x);
         const float2 w = e.w[i];
         e.prev[i] = a1;
-        e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+        e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
+                             fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
     } else {
         // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
         const float2 am = e.prev[i];
         const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
         const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
         float2 s = e.S[i];
-        s.x = fmaf(e.c1, an.x, s.x) * att;
-        s.y = fmaf(e.c1, an.y, s.y) * att;
+        s.x = fmaf(e.c1, an.x, fmaf(e.c1l, an.x, s.x)) * att;
+        s.y = fmaf(e.c1, an.y, fmaf(e.c1l, an.y, s.y)) * att;
         if (EPI == EPI_MID) {
             e.prev[i] = an;
             e.S[i] = s;
@@ -371,13 +373,16 @@ cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const 
 
 cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                   const AxisPlan& py, const AxisPlan& pz, const Tables& t,
-                                  const float2* in, float2* X, float2* out, const float* vs)
+                                  const float2* in, float2* X, float2* out, const float* vs,
+                                  float sch, float scl)
 {
     cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, in, X, nullptr);
     if (err != cudaSuccess) return err;
     EpiArgs e{};
     e.prev = out;
     e.vs = vs;
+    e.sch = sch;
+    e.scl = scl;
     const long long nrows = (long long)g.nyb * g.nzb;
     const int rpc = rows_per_cta(px.n);
     k_rows<true, EPI_SCALE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
@@ -408,20 +413,20 @@ cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float*
     return cudaGetLastError();
 }
 
-// The generic operator with the velocity and 1/(R N) given separately, for
-// callers that hold a plain velocity array: out = vel * scale * IFFT3(|k| FFT3(in)).
+// The generic operator for callers that hold a plain velocity array and pass
+// the scale: out = vel * scale * IFFT3(|k| FFT3(in)).
 // X is caller-provided scratch of one field.
 cudaError_t launch_apply_operator_vel(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                       const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                       const float2* in, float2* X, float2* out, const float* vel,
-                                      float scale)
+                                      double scale)
 {
     cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, in, X, nullptr);
     if (err != cudaSuccess) return err;
     EpiArgs e{};
     e.prev = out;
     e.vs = vel;
-    e.c0 = scale;
+    split_float(scale, &e.sch, &e.scl);
     const long long nrows = (long long)g.nyb * g.nzb;
     const int rpc = rows_per_cta(px.n);
     k_rows<true, EPI_SCALE_VEL><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(

@@ -33,7 +33,7 @@ namespace ose {
 cudaError_t launch_apply_operator_vel(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                       const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                       const float2* in, float2* X, float2* out, const float* vel,
-                                      float scale);
+                                      double scale);
 
 namespace {
 
@@ -104,8 +104,14 @@ extern "C" ose_status ose_apply_operator_noalloc(int nxb, int nyb, int nzb, floa
         tw, k2, nxb, nyb, nzb, pi2 / dx / nxb, pi2 / dy / nyb, pi2 / dz / nzb);
     if (cudaGetLastError() != cudaSuccess) return OSE_ERR_CUDA;
     Geometry g{nxb, nyb, nzb, (long long)nxb * nyb * nzb};
-    Tables t{tw, tw + kMaxAxisLen, tw + 2 * kMaxAxisLen, k2, k2 + kMaxAxisLen, k2 + 2 * kMaxAxisLen};
-    const float scale = (float)(1.0 / (R * (double)g.ncell));
+    Tables t{};
+    t.twx = tw;
+    t.twy = tw + kMaxAxisLen;
+    t.twz = tw + 2 * kMaxAxisLen;
+    t.kx2 = k2;
+    t.ky2 = k2 + kMaxAxisLen;
+    t.kz2 = k2 + 2 * kMaxAxisLen;
+    const double scale = 1.0 / (R * (double)g.ncell);
     cudaError_t e = launch_apply_operator_vel(s, g, px, py, pz, t, reinterpret_cast<const float2*>(in), base,
                                               reinterpret_cast<float2*>(out), vel, scale);
     return e == cudaSuccess ? OSE_OK : OSE_ERR_CUDA;

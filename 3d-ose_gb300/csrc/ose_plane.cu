@@ -38,7 +38,7 @@ constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
-constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + N;   // + twiddle table
+constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N;   // + twiddle table (hi, lo)
 constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX;
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -69,23 +69,39 @@ __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2&
     a3 = csub(t1, t3);
 }
 
-// times W_16^E (forward) or its conjugate (inverse); E in {0,1,2,3,4,6,9}
+// times W_16^E (forward) or its conjugate (inverse); E in {0,1,2,3,4,6,9}.
+// The constants are float pairs hi + lo (cos(pi/8), sin(pi/8), sqrt(1/2) to
+// about 48 bits): a rounded constant would perturb every transform the same
+// way, and that bias adds up coherently over thousands of steps.
 template <int E, bool INV>
 __device__ __forceinline__ float2 w16(float2 a)
 {
-    constexpr float C1 = 0.923879532511286756f;   // cos(pi/8)
-    constexpr float S1 = 0.382683432365089772f;   // sin(pi/8)
-    constexpr float H = 0.707106781186547524f;    // sqrt(1/2)
+    constexpr double C1d = 0.92387953251128675612818318939678828682;   // cos(pi/8)
+    constexpr double S1d = 0.38268343236508977172845998403039886676;   // sin(pi/8)
+    constexpr double Hd = 0.70710678118654752440084436210484903928;    // sqrt(1/2)
+    constexpr float C1 = (float)C1d, C1l = (float)(C1d - (double)(float)C1d);
+    constexpr float S1 = (float)S1d, S1l = (float)(S1d - (double)(float)S1d);
+    constexpr float H = (float)Hd, Hl = (float)(Hd - (double)(float)Hd);
     constexpr float s = INV ? 1.f : -1.f;         // sign of the sine part
     if (E == 0) return a;
     if (E == 4) return rot<INV>(a);
-    float c, sn;
-    if (E == 1) { c = C1; sn = s * S1; }
-    else if (E == 2) { c = H; sn = s * H; }
-    else if (E == 3) { c = S1; sn = s * C1; }
-    else if (E == 6) { c = -H; sn = s * H; }
-    else { c = -C1; sn = -s * S1; }   // E == 9
-    return make_float2(fmaf(a.x, c, -a.y * sn), fmaf(a.x, sn, a.y * c));
+    float c, cl, sn, snl;
+    if (E == 1) { c = C1; cl = C1l; sn = s * S1; snl = s * S1l; }
+    else if (E == 2) { c = H; cl = Hl; sn = s * H; snl = s * Hl; }
+    else if (E == 3) { c = S1; cl = S1l; sn = s * C1; snl = s * C1l; }
+    else if (E == 6) { c = -H; cl = -Hl; sn = s * H; snl = s * Hl; }
+    else { c = -C1; cl = -C1l; sn = -s * S1; snl = -s * S1l; }   // E == 9
+    const float tx = fmaf(a.x, cl, -a.y * snl), ty = fmaf(a.x, snl, a.y * cl);
+    return make_float2(fmaf(a.x, c, fmaf(-a.y, sn, tx)), fmaf(a.x, sn, fmaf(a.y, c, ty)));
+}
+
+// a * (w + wl) with w, wl the two halves of a twiddle (conj for INV)
+template <bool INV>
+__device__ __forceinline__ float2 cmul_ff(float2 a, float2 w, float2 wl)
+{
+    if (INV) { w.y = -w.y; wl.y = -wl.y; }
+    const float tx = fmaf(a.x, wl.x, -a.y * wl.y), ty = fmaf(a.x, wl.y, a.y * wl.x);
+    return make_float2(fmaf(a.x, w.x, fmaf(-a.y, w.y, tx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ty)));
 }
 
 // In-register 16-point DFT, natural order in and out (4 x 4 split).
@@ -185,7 +201,7 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
         const int j = ROWS ? row_slot(s).j : col_slot(s).j;
         dft16<INV>(v);
 #pragma unroll
-        for (int k = 1; k < 16; ++k) v[k] = INV ? cmulc(v[k], tw[j * k]) : cmul(v[k], tw[j * k]);
+        for (int k = 1; k < 16; ++k) v[k] = cmul_ff<INV>(v[k], tw[j * k], tw[N + j * k]);
     }
     exchange<ROWS>(T, v0, v1);
     dft16<INV>(v0);
@@ -195,16 +211,21 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
 struct Args {
     const float2* src;     // k_plane_fwd: state rows.  k_plane_inv: spectrum after k_zpass
     float2* dst;           // spectrum of the next application (forward output)
-    const float2* tw;      // W_256^t, t < 256
+    const float2* tw;      // W_256^t, t < 256 (nearest floats)
+    const float2* twl;     // remainders of the twiddles
     const float* kx2;
     const float* ky2;
     const float* kz2;
     EpiArgs e;
 };
 
-__device__ __forceinline__ void load_twiddles(float2* tw, const float2* g)
+// W_256^t, t < 256, at tw[t] (nearest floats) and tw[256 + t] (remainders)
+__device__ __forceinline__ void load_twiddles(float2* tw, const float2* g, const float2* gl)
 {
-    for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = g[t];
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        tw[t] = g[t];
+        tw[N + t] = gl[t];
+    }
 }
 
 // Bulk prefetch of a contiguous range into L2 (no registers, no shared
@@ -258,11 +279,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 {
     extern __shared__ float4 smem4[];
     float2* smem = reinterpret_cast<float2*>(smem4);
-    float2* tw = smem + (SMEM_COMPLEX - N);
+    float2* tw = smem + (SMEM_COMPLEX - 2 * N);
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
-    load_twiddles(tw, a.tw);
+    load_twiddles(tw, a.tw, a.twl);
     float2 v0[16], v1[16];
     const float2* in = a.src + ((size_t)z * N + SL * r) * N;
 #pragma unroll
@@ -311,22 +332,25 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
             const int n1 = 8 * h + q;
             const int x = 16 * n1 + j;
             const size_t i = rowbase + 16 * n1;
-            const float2 Lx = make_float2(v[n1].x * vv[q], v[n1].y * vv[q]);
+            // L a_n = v * X * (sch + scl)
+            float2 Lx = make_float2(v[n1].x * vv[q], v[n1].y * vv[q]);
+            Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
             if (EPI == EPI_SCALE) {
                 prev[i] = Lx;
             } else if (EPI == EPI_FIRST) {
                 // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1
                 const float2 a1 = make_float2(Lx.y, -Lx.x);
                 prev[i] = a1;
-                S[i] = make_float2(fmaf(e.c0, am[q].x, e.c1 * a1.x), fmaf(e.c0, am[q].y, e.c1 * a1.y));
+                S[i] = make_float2(fmaf(e.c0, am[q].x, fmaf(e.c1, a1.x, fmaf(e.c0l, am[q].x, e.c1l * a1.x))),
+                                   fmaf(e.c0, am[q].y, fmaf(e.c1, a1.y, fmaf(e.c0l, am[q].y, e.c1l * a1.y))));
                 v[n1] = a1;
             } else {
                 // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
                 const float att = __ldg(e.ax + x) * attyz;
                 float2 s = sm[q];
-                s.x = fmaf(e.c1, an.x, s.x) * att;
-                s.y = fmaf(e.c1, an.y, s.y) * att;
+                s.x = fmaf(e.c1, an.x, fmaf(e.c1l, an.x, s.x)) * att;
+                s.y = fmaf(e.c1, an.y, fmaf(e.c1l, an.y, s.y)) * att;
                 if (EPI == EPI_MID) {
                     prev[i] = an;
                     S[i] = s;
@@ -353,7 +377,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 {
     extern __shared__ float4 smem4[];
     float2* smem = reinterpret_cast<float2*>(smem4);
-    float2* tw = smem + (SMEM_COMPLEX - N);
+    float2* tw = smem + (SMEM_COMPLEX - 2 * N);
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
@@ -369,7 +393,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
             prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
         }
     }
-    load_twiddles(tw, a.tw);
+    load_twiddles(tw, a.tw, a.twl);
     float2 v0[16], v1[16];
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
     const float2* in = a.src + (size_t)z * N * N + SL * r;
@@ -417,17 +441,26 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 // One line slot per thread (column c = t % 16, line thread j = t / 16) keeps
 // registers near 64 so four CTAs share an SM.
 constexpr int ZW = 16;
-constexpr size_t ZSMEM_BYTES = sizeof(float2) * (16 * 16 * ZW + N);
+constexpr int ZTHREADS = 256;
+constexpr size_t ZSMEM_BYTES = sizeof(float2) * (16 * 16 * ZW + 2 * N);
 
-__global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
-                                                        const float* __restrict__ kx2,
-                                                        const float* __restrict__ ky2,
-                                                        const float* __restrict__ kz2)
+// (hi, lo) + (hi, lo) as a float pair (Knuth's two-sum on the high parts)
+__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float& h, float& l)
+{
+    const float s = ah + bh;
+    const float bb = s - ah;
+    const float e = (ah - (s - bb)) + (bh - bb);
+    h = s;
+    l = e + al + bl;
+}
+
+__global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
+                                                         Tables t)
 {
     extern __shared__ float4 smem4[];
     float2* T = reinterpret_cast<float2*>(smem4);
     float2* tw = T + 16 * 16 * ZW;
-    load_twiddles(tw, gtw);
+    load_twiddles(tw, gtw, t.twl);
     const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
     const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
     float2* base = X + (size_t)ky * N + kx;
@@ -439,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, 
     // forward: DFT16 over n1, twiddle, transpose, DFT16 over n2
     dft16<false>(v);
 #pragma unroll
-    for (int k = 1; k < 16; ++k) v[k] = cmul(v[k], tw[j * k]);
+    for (int k = 1; k < 16; ++k) v[k] = cmul_ff<false>(v[k], tw[j * k], tw[N + j * k]);
 #pragma unroll
     for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
     __syncthreads();
@@ -447,18 +480,24 @@ __global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, 
     for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
     __syncthreads();
     dft16<false>(v);
-    // v[k2] = spectrum at kz = j + 16 k2
-    const float kxy = __ldg(kx2 + kx) + __ldg(ky2 + ky);
+    // v[k2] = spectrum at kz = j + 16 k2; scale by |k| to about 44 bits:
+    // k^2 as a float pair, sqrt of its high part, one Newton correction.
+    float kxyh, kxyl;
+    ff_add(__ldg(t.kx2 + kx), __ldg(t.kx2l + kx), __ldg(t.ky2 + ky), __ldg(t.ky2l + ky), kxyh, kxyl);
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
-        const float k = sqrtf(kxy + __ldg(kz2 + j + 16 * k2));
-        v[k2].x *= k;
-        v[k2].y *= k;
+        const int kz = j + 16 * k2;
+        float sh, sl;
+        ff_add(kxyh, kxyl, __ldg(t.kz2 + kz), __ldg(t.kz2l + kz), sh, sl);
+        const float r = sqrtf(sh);
+        const float e = fmaf(-r, r, sh) + sl;
+        const float rl = r > 0.f ? 0.5f * e / r : 0.f;
+        v[k2] = make_float2(fmaf(v[k2].x, r, v[k2].x * rl), fmaf(v[k2].y, r, v[k2].y * rl));
     }
     // inverse: IDFT16 over k2, twiddle, transpose, IDFT16 over k1
     dft16<true>(v);
 #pragma unroll
-    for (int k = 1; k < 16; ++k) v[k] = cmulc(v[k], tw[j * k]);
+    for (int k = 1; k < 16; ++k) v[k] = cmul_ff<true>(v[k], tw[j * k], tw[N + j * k]);
 #pragma unroll
     for (int k = 0; k < 16; ++k) T[(j * 16 + k) * ZW + c] = v[k];
     __syncthreads();
@@ -467,51 +506,6 @@ __global__ void __launch_bounds__(THREADS, 4) k_zpass16(float2* __restrict__ X, 
     dft16<true>(v);
 #pragma unroll
     for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + j) * plane] = v[n1];
-}
-
-// z lines of a 32-wide kx tile at one ky: forward, * |k|, inverse, in place.
-__global__ void __launch_bounds__(THREADS, 2) k_zpass(float2* X, const float2* gtw, const float* kx2,
-                                                      const float* ky2, const float* kz2)
-{
-    extern __shared__ float4 smem4[];
-    float2* smem = reinterpret_cast<float2*>(smem4);
-    float2* tw = smem + (SMEM_COMPLEX - N);
-    load_twiddles(tw, gtw);
-    const int ky = blockIdx.y;
-    const int kx0 = SL * blockIdx.x;
-    float2* base = X + (size_t)ky * N + kx0;
-    const size_t plane = (size_t)N * N;
-    float2 v0[16], v1[16];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const ColSlot q = col_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + q.j) * plane + q.c];
-    }
-    __syncthreads();
-    fft256<false, false>(smem, tw, v0, v1);
-    const float kyy = __ldg(ky2 + ky);
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const ColSlot q = col_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-        const float kxy = __ldg(kx2 + kx0 + q.c) + kyy;
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2) {
-            const float k = sqrtf(kxy + __ldg(kz2 + q.j + 16 * k2));
-            v[k2].x *= k;
-            v[k2].y *= k;
-        }
-    }
-    fft256<true, false>(smem, tw, v0, v1);
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const ColSlot q = col_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + q.j) * plane + q.c] = v[n1];
-    }
 }
 
 }  // namespace plane
@@ -535,38 +529,38 @@ cudaError_t configure_plane_kernels()
     ALLOW((plane::k_plane_inv<EPI_LAST, false>));
     ALLOW((plane::k_plane_inv<EPI_MID, false>));
     ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
-    ALLOW(plane::k_zpass);
     ALLOW(plane::k_zpass16);
 #undef ALLOW
     return cudaSuccess;
 }
 
-cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const float2* tw)
+cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const Tables& t)
 {
     plane::Args a{};
     a.src = state;
     a.dst = X;
-    a.tw = tw;
+    a.tw = t.twx;
+    a.twl = t.twl;
     plane::k_plane_fwd<<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_zpass(cudaStream_t s, float2* X, const float2* tw, const Tables& t)
+cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
 {
-    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::THREADS, plane::ZSMEM_BYTES, s>>>(
-        X, tw, t.kx2, t.ky2, t.kz2);
+    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(X, t.twx, t);
     return cudaGetLastError();
 }
 
 // mode: EPI_FIRST / EPI_MID with the next forward fused (fwd = true), or
 // EPI_LAST without it.  Xin: spectrum after the z pass; Xout: next spectrum.
 cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float2* Xin, float2* Xout,
-                             const float2* tw, const EpiArgs& e)
+                             const Tables& t, const EpiArgs& e)
 {
     plane::Args a{};
     a.src = Xin;
     a.dst = Xout;
-    a.tw = tw;
+    a.tw = t.twx;
+    a.twl = t.twl;
     a.e = e;
     const dim3 grid(plane::CL, plane::N);
     if (mode == EPI_FIRST)
@@ -580,18 +574,21 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     return cudaGetLastError();
 }
 
-// out = v * IFFT3(|k| FFT3(in)) / (R N) with the plane kernels.
+// out = v * IFFT3(|k| FFT3(in)) * (sch + scl) with the plane kernels.
 cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
-                                        const float* vs, const float2* tw, const Tables& t)
+                                        const float* vs, float sch, float scl, const Tables& t)
 {
-    cudaError_t e = launch_plane_fwd(s, in, X, tw);
+    cudaError_t e = launch_plane_fwd(s, in, X, t);
     if (e != cudaSuccess) return e;
-    if ((e = launch_zpass(s, X, tw, t)) != cudaSuccess) return e;
+    if ((e = launch_zpass(s, X, t)) != cudaSuccess) return e;
     plane::Args a{};
     a.src = X;
-    a.tw = tw;
+    a.tw = t.twx;
+    a.twl = t.twl;
     a.e.prev = out;
     a.e.vs = vs;
+    a.e.sch = sch;
+    a.e.scl = scl;
     plane::k_plane_inv<EPI_SCALE, false><<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
     return cudaGetLastError();
 }
