@@ -33,7 +33,10 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
            "ose_profile_step", "ose_write_outputs", "ose_version", "ose_apply_operator_noalloc",
            "ose_checkpoint_save", "ose_checkpoint_load", "ose_run_snapshots", "ose_write_su",
-           "ose_write_segy"]
+           "ose_write_segy", "ose_batch_create", "ose_batch_destroy", "ose_batch_last_error",
+           "ose_batch_reset", "ose_batch_run", "ose_batch_run_timed", "ose_batch_info",
+           "ose_batch_get_gather", "ose_batch_get_wavefield", "ose_batch_autotune",
+           "ose_batch_get_tuning"]
 
 # void (*)(int it, const float* P, const float* Q, void* user)
 SNAPSHOT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
@@ -126,6 +129,19 @@ def load_library(path: str = LIB_PATH):
                               ctypes.c_int),
         "ose_write_su": ([H, ctypes.c_char_p], ctypes.c_int),
         "ose_write_segy": ([H, ctypes.c_char_p], ctypes.c_int),
+        "ose_batch_create": ([P(Params), f32, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              P(ShotWindow), P(H)], ctypes.c_int),
+        "ose_batch_destroy": ([H], ctypes.c_int),
+        "ose_batch_last_error": ([H], ctypes.c_char_p),
+        "ose_batch_reset": ([H], ctypes.c_int),
+        "ose_batch_run": ([H, ctypes.c_int], ctypes.c_int),
+        "ose_batch_run_timed": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_batch_info": ([H, ctypes.c_int, P(Derived), P(ctypes.c_longlong)], ctypes.c_int),
+        "ose_batch_get_gather": ([H, ctypes.c_int, f32], ctypes.c_int),
+        "ose_batch_get_wavefield": ([H, ctypes.c_int, ctypes.c_int, f32], ctypes.c_int),
+        "ose_batch_autotune": ([H, ctypes.c_int, ctypes.c_char_p, f32], ctypes.c_int),
+        "ose_batch_get_tuning": ([H, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)],
+                                 ctypes.c_int),
         "ose_apply_operator_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                         ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -161,6 +177,96 @@ def default_params(**kw) -> Params:
 
 def _f32(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class ShotWindow(ctypes.Structure):
+    """ose_shot_window (include/ose3d.h)."""
+
+    _fields_ = [(k, ctypes.c_int) for k in ("x0", "y0", "z0", "nx", "ny", "nz", "sx", "sy", "sz")]
+
+
+class Batch:
+    """Many shots on windows of one model, advanced together (ose_batch_*)."""
+
+    def __init__(self, params: Params, model_xyz: np.ndarray, windows):
+        self._lib = load_library()
+        m = np.ascontiguousarray(model_xyz, dtype=np.float32)
+        if m.ndim != 3:
+            raise ValueError("model must be a 3-D [x][y][z] array")
+        arr = (ShotWindow * len(windows))()
+        for i, w in enumerate(windows):
+            for k in ("x0", "y0", "z0", "nx", "ny", "nz", "sx", "sy", "sz"):
+                setattr(arr[i], k, int(w[k]))
+        h = ctypes.c_void_p()
+        st = self._lib.ose_batch_create(ctypes.byref(params), _f32(m), m.shape[0], m.shape[1], m.shape[2],
+                                        len(windows), arr, ctypes.byref(h))
+        if st != OK:
+            raise OseError(st, self._lib.ose_batch_last_error(None).decode())
+        self._h = h
+        self.params = params
+        self.nshots = len(windows)
+        self.windows = [dict(w) for w in windows]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ose_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != OK:
+            raise OseError(st, self._lib.ose_batch_last_error(self._h).decode())
+
+    def reset(self):
+        self._check(self._lib.ose_batch_reset(self._h))
+
+    def run(self, nsteps: int):
+        self._check(self._lib.ose_batch_run(self._h, nsteps))
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = ctypes.c_float()
+        self._check(self._lib.ose_batch_run_timed(self._h, nsteps, ctypes.byref(ms)))
+        return ms.value
+
+    def info(self, shot: int):
+        d = Derived()
+        cells = ctypes.c_longlong()
+        self._check(self._lib.ose_batch_info(self._h, shot, ctypes.byref(d), ctypes.byref(cells)))
+        return d, cells.value
+
+    def gather(self, shot: int) -> np.ndarray:
+        w = self.windows[shot]
+        g = np.zeros((w["nx"] * w["ny"], self.params.nt), np.float32)
+        self._check(self._lib.ose_batch_get_gather(self._h, shot, _f32(g)))
+        return g
+
+    def wavefield(self, shot: int, which: int = FIELD_Q) -> np.ndarray:
+        d, _ = self.info(shot)
+        out = np.zeros((d.nzb, d.nyb, d.nxb), np.float32)
+        self._check(self._lib.ose_batch_get_wavefield(self._h, shot, which, _f32(out)))
+        return out
+
+    def autotune(self, steps: int = 3, cache_path: str | None = None) -> float:
+        ms = ctypes.c_float()
+        self._check(self._lib.ose_batch_autotune(self._h, steps, cache_path.encode() if cache_path else None,
+                                                 ctypes.byref(ms)))
+        return ms.value
+
+    def tuning(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        self._check(self._lib.ose_batch_get_tuning(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("rows_scale", "txy", "txz", "radix_order"), (x.value for x in v)))
 
 
 class Modeler:

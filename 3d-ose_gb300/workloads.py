@@ -61,3 +61,33 @@ CONFIGS = {
                     fm=20.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
                     sxbeg=50, sybeg=50, szbeg=10, gzbeg=5)),
 }
+
+
+def batched_windows(nshots: int = 64, seed: int = 64, model_shape=(512, 512, 192), sponge: int = 16,
+                    depth: int = 5):
+    """Shot windows of the batched workload: sources on a seeded grid of
+    sqrt(nshots) x sqrt(nshots) surface positions, each shot on a window centred
+    on its source whose PADDED size (interior + 2 * sponge) is drawn from
+    96..192 (x, y) and 128..192 (z) in steps of 16."""
+    rng = np.random.default_rng(seed)
+    mx, my, mz = model_shape
+    g = int(round(nshots ** 0.5))
+    wins = []
+    for s in range(nshots):
+        i, j = s % g, s // g
+        sx = int((i + 0.5) * mx / g + rng.integers(-8, 9))
+        sy = int((j + 0.5) * my / g + rng.integers(-8, 9))
+        nxp = int(rng.choice(np.arange(96, 193, 16)))
+        nyp = int(rng.choice(np.arange(96, 193, 16)))
+        nzp = int(rng.choice(np.arange(128, 193, 16)))
+        nx, ny, nz = nxp - 2 * sponge, nyp - 2 * sponge, nzp - 2 * sponge
+        x0, y0 = sx - nx // 2, sy - ny // 2
+        wins.append(dict(x0=x0, y0=y0, z0=0, nx=nx, ny=ny, nz=nz, sx=sx - x0, sy=sy - y0, sz=depth))
+    return wins
+
+
+# 64 shots on a 512 x 512 x 192 model, windows 96..192 cells, dt 2 ms, 1200 steps
+BATCHED = dict(model=lambda: smooth_random_salt(512, 512, 192, seed=77),
+               params=dict(bu=16, bd=16, bl=16, br=16, bf=16, bb=16, nt=1200, fm=20.0, dt=0.002,
+                           amp=100.0, dx=10.0, dy=10.0, dz=10.0, gzbeg=0),
+               windows=lambda: batched_windows())

@@ -238,6 +238,53 @@ ose_status ose_run_snapshots(ose_handle* h, int nsteps, int every, int layout,
 ose_status ose_write_su(ose_handle* h, const char* path);
 ose_status ose_write_segy(ose_handle* h, const char* path);
 
+/* ---- batched shots -------------------------------------------------------
+ * The reference loops over shots one after another on the full model
+ * (for(is...) in ose_3d.cu:242-279, nshot = 1 there).  A batch gives every
+ * shot its own window of the model around its source and advances all
+ * windows together: each pass of a time step is one launch over every shot,
+ * and a step is one CUDA graph. */
+
+/* One shot of a batch.  The window interior is model cells
+ * [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) (cells outside the model repeat its
+ * edge); the shot pads it with the sponge widths of the batch parameters
+ * (judge_odd applies).  (sx, sy, sz): source cell inside the window
+ * interior.  Receivers: every interior (x, y) of the window at depth gzbeg. */
+typedef struct ose_shot_window {
+    int x0, y0, z0;
+    int nx, ny, nz;
+    int sx, sy, sz;
+} ose_shot_window;
+
+typedef struct ose_batch ose_batch;
+
+/* p: shared parameters (sponge widths, nt, fm, dt, amp, dx..dz, gzbeg,
+ * switches; its nx..nz and source fields are ignored).  model: mnx*mny*mnz
+ * floats in the reference layout [x][y][z].  Each shot has its own velocity
+ * window, vmax, R, series order M and tables (ose_batch_info). */
+ose_status ose_batch_create(const ose_params* p, const float* model, int mnx, int mny, int mnz,
+                            int nshots, const ose_shot_window* windows, ose_batch** out);
+ose_status ose_batch_destroy(ose_batch* b);
+const char* ose_batch_last_error(const ose_batch* b);
+/* All shots back to rest at step 0. */
+ose_status ose_batch_reset(ose_batch* b);
+/* nsteps steps of every shot (graph replays). */
+ose_status ose_batch_run(ose_batch* b, int nsteps);
+/* As ose_batch_run, timed with CUDA events on the batch's stream. */
+ose_status ose_batch_run_timed(ose_batch* b, int nsteps, float* ms);
+/* Derived values and padded cell count of one shot. */
+ose_status ose_batch_info(const ose_batch* b, int shot, ose_derived* d, long long* cells);
+/* One shot's gather, [ig][it] (nx*ny x nt floats of its window). */
+ose_status ose_batch_get_gather(ose_batch* b, int shot, float* out);
+/* One shot's padded P or Q, [z][y][x]. */
+ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out);
+/* Pick the rows per x-pass block, the y/z column tile widths and the radix
+ * order by timing candidates over `steps` steps (coordinate search); reuse a
+ * cached choice for the same window sizes from cache_path (a text file, one
+ * line per batch shape; NULL = no cache).  Resets the batch. */
+ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, float* best_ms);
+ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order);
+
 /* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
 #define OSE_NOALLOC_MAX_CELLS 262144
 
