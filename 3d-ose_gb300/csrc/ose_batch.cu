@@ -327,7 +327,10 @@ ose_status ose_batch_create(const ose_params* p, const float* model, int mnx, in
         auto up = [&](void* dst, const void* src, size_t bytes) {
             return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->stream);
         };
-        BCKC(up(vs, sh.vb.data(), sizeof(float) * N));
+        std::vector<float> vsc(sh.vb);
+        if (!ose::kCompensatedConstants)
+            for (size_t i = 0; i < N; ++i) vsc[i] = (float)((double)sh.vb[i] / (d.R * (double)N));
+        BCKC(up(vs, vsc.data(), sizeof(float) * N));
         BCKC(up(rk, ricker.data(), sizeof(float) * p->nt));
         BCKC(up(hl, hil.data(), sizeof(float) * p->nt));
         BCKC(up(tw[0], t0.data(), sizeof(float2) * d.nxb));

@@ -437,7 +437,14 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(dalloc(h, &h->hil, (size_t)p.nt));
     CKC(dalloc(h, &h->gather, (size_t)p.nt * d.ng));
     CKC(dalloc(h, &h->ctr, 4));
-    CKC(upload(h, h->vs, h->vb));
+    if (ose::kCompensatedConstants) {
+        CKC(upload(h, h->vs, h->vb));
+    } else {
+        std::vector<float> vsc(N);
+        const double sc = 1.0 / (d.R * (double)N);
+        for (size_t i = 0; i < N; ++i) vsc[i] = (float)((double)h->vb[i] * sc);
+        CKC(upload(h, h->vs, vsc));
+    }
     CKC(upload(h, h->twxl, twxl));
     CKC(upload(h, h->kx2l, kx2l));
     CKC(upload(h, h->ky2l, ky2l));

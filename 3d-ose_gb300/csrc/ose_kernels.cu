@@ -139,7 +139,9 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
 {
     const float v = __ldg(e.vs + i);
     float2 Lx = cscale(X, v);
-    Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
+    // compensated: vs holds v and (sch + scl) = 1/(R N); else vs holds v/(R N)
+    if (kCompensatedConstants || EPI == EPI_SCALE_VEL)
+        Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
     if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
         e.prev[i] = Lx;
     } else if (EPI == EPI_FIRST) {
@@ -147,16 +149,23 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
         const float2 a1 = make_float2(Lx.y, -Lx.x);
         const float2 w = e.w[i];
         e.prev[i] = a1;
-        e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
-                             fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
+        if (kCompensatedConstants)
+            e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
+                                 fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
+        else
+            e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
     } else {
         // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
         const float2 am = e.prev[i];
         const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
         const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
         float2 s = e.S[i];
-        s.x = fmaf(e.c1, an.x, fmaf(e.c1l, an.x, s.x)) * att;
-        s.y = fmaf(e.c1, an.y, fmaf(e.c1l, an.y, s.y)) * att;
+        if (kCompensatedConstants) {
+            s.x = fmaf(e.c1l, an.x, s.x);
+            s.y = fmaf(e.c1l, an.y, s.y);
+        }
+        s.x = fmaf(e.c1, an.x, s.x) * att;
+        s.y = fmaf(e.c1, an.y, s.y) * att;
         if (EPI == EPI_MID) {
             e.prev[i] = an;
             e.S[i] = s;

@@ -339,25 +339,33 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
             const int n1 = 8 * h + q;
             const int x = 16 * n1 + j;
             const size_t i = rowbase + 16 * n1;
-            // L a_n = v * X * (sch + scl)
+            // L a_n = v * X * (sch + scl)  (vv = v / (R N) when not compensated)
             float2 Lx = make_float2(v[n1].x * vv[q], v[n1].y * vv[q]);
-            Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
+            if (kCompensatedConstants)
+                Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
             if (EPI == EPI_SCALE) {
                 prev[i] = Lx;
             } else if (EPI == EPI_FIRST) {
                 // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1
                 const float2 a1 = make_float2(Lx.y, -Lx.x);
                 prev[i] = a1;
-                S[i] = make_float2(fmaf(e.c0, am[q].x, fmaf(e.c1, a1.x, fmaf(e.c0l, am[q].x, e.c1l * a1.x))),
-                                   fmaf(e.c0, am[q].y, fmaf(e.c1, a1.y, fmaf(e.c0l, am[q].y, e.c1l * a1.y))));
+                if (kCompensatedConstants)
+                    S[i] = make_float2(fmaf(e.c0, am[q].x, fmaf(e.c1, a1.x, fmaf(e.c0l, am[q].x, e.c1l * a1.x))),
+                                       fmaf(e.c0, am[q].y, fmaf(e.c1, a1.y, fmaf(e.c0l, am[q].y, e.c1l * a1.y))));
+                else
+                    S[i] = make_float2(fmaf(e.c0, am[q].x, e.c1 * a1.x), fmaf(e.c0, am[q].y, e.c1 * a1.y));
                 v[n1] = a1;
             } else {
                 // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
                 const float att = __ldg(e.ax + x) * attyz;
                 float2 s = sm[q];
-                s.x = fmaf(e.c1, an.x, fmaf(e.c1l, an.x, s.x)) * att;
-                s.y = fmaf(e.c1, an.y, fmaf(e.c1l, an.y, s.y)) * att;
+                if (kCompensatedConstants) {
+                    s.x = fmaf(e.c1l, an.x, s.x);
+                    s.y = fmaf(e.c1l, an.y, s.y);
+                }
+                s.x = fmaf(e.c1, an.x, s.x) * att;
+                s.y = fmaf(e.c1, an.y, s.y) * att;
                 if (EPI == EPI_MID) {
                     prev[i] = an;
                     S[i] = s;
@@ -487,19 +495,29 @@ __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X,
     for (int a = 0; a < 16; ++a) v[a] = T[(a * 16 + j) * ZW + c];
     __syncthreads();
     dft16<false>(v);
-    // v[k2] = spectrum at kz = j + 16 k2; scale by |k| to about 44 bits:
-    // k^2 as a float pair, sqrt of its high part, one Newton correction.
-    float kxyh, kxyl;
-    ff_add(__ldg(t.kx2 + kx), __ldg(t.kx2l + kx), __ldg(t.ky2 + ky), __ldg(t.ky2l + ky), kxyh, kxyl);
+    // v[k2] = spectrum at kz = j + 16 k2.  Compensated: |k| to about 44 bits
+    // (k^2 as a float pair, sqrt of its high part, one Newton correction).
+    if (kCompensatedConstants) {
+        float kxyh, kxyl;
+        ff_add(__ldg(t.kx2 + kx), __ldg(t.kx2l + kx), __ldg(t.ky2 + ky), __ldg(t.ky2l + ky), kxyh, kxyl);
 #pragma unroll
-    for (int k2 = 0; k2 < 16; ++k2) {
-        const int kz = j + 16 * k2;
-        float sh, sl;
-        ff_add(kxyh, kxyl, __ldg(t.kz2 + kz), __ldg(t.kz2l + kz), sh, sl);
-        const float r = sqrtf(sh);
-        const float e = fmaf(-r, r, sh) + sl;
-        const float rl = r > 0.f ? 0.5f * e / r : 0.f;
-        v[k2] = make_float2(fmaf(v[k2].x, r, v[k2].x * rl), fmaf(v[k2].y, r, v[k2].y * rl));
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const int kz = j + 16 * k2;
+            float sh, sl;
+            ff_add(kxyh, kxyl, __ldg(t.kz2 + kz), __ldg(t.kz2l + kz), sh, sl);
+            const float r = sqrtf(sh);
+            const float e = fmaf(-r, r, sh) + sl;
+            const float rl = r > 0.f ? 0.5f * e / r : 0.f;
+            v[k2] = make_float2(fmaf(v[k2].x, r, v[k2].x * rl), fmaf(v[k2].y, r, v[k2].y * rl));
+        }
+    } else {
+        const float kxy = __ldg(t.kx2 + kx) + __ldg(t.ky2 + ky);
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const float k = sqrtf(kxy + __ldg(t.kz2 + j + 16 * k2));
+            v[k2].x *= k;
+            v[k2].y *= k;
+        }
     }
     // inverse: IDFT16 over k2, twiddle, transpose, IDFT16 over k1
     dft16<true>(v);
