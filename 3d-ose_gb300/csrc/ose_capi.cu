@@ -43,6 +43,10 @@ struct ose_handle {
     float* gather = nullptr; // [nt][ng]
     int* ctr = nullptr;      // [0] next step, [1] current step
     size_t bytes = 0;
+    // precision form: mode, DFT operands of the tensor-core z pass, error word
+    int precision = OSE_PRECISION_FP32;
+    void* tcb = nullptr;
+    int* tcerr = nullptr;
 
     // host copies
     std::vector<float> vb, h_ax, h_ay, h_az, h_ricker, h_hil;
@@ -107,7 +111,7 @@ void free_all(ose_handle* h)
     if (h->graph) cudaGraphExecDestroy(h->graph);
     void* bufs[] = {h->W, h->A, h->S, h->X, h->vs, h->ax, h->ay, h->az, h->kx2, h->ky2, h->kz2,
                     h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr,
-                    h->kx2l, h->ky2l, h->kz2l, h->twxl};
+                    h->kx2l, h->ky2l, h->kz2l, h->twxl, h->tcb, h->tcerr};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -268,6 +272,20 @@ ose_status build_graph(ose_handle* h)
 
 ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVALID; }
 
+// After the stream is idle: the tensor-core z pass records a wait that ran out
+// of time in its error word (the kernel then leaves its columns unchanged).
+ose_status tensor_status(ose_handle* h)
+{
+    if (h->precision == OSE_PRECISION_FP32 || !h->tcerr) return OSE_OK;
+    int v = 0;
+    CK(h, cudaMemcpy(&v, h->tcerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+        CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
+        return fail(h, OSE_ERR_CUDA, "tensor-core z pass: an MMA completion wait ran out of time");
+    }
+    return OSE_OK;
+}
+
 void to_layout(const ose_handle* h, const float* zyx, float* out, int layout)
 {
     const int nxb = h->d.nxb, nyb = h->d.nyb, nzb = h->d.nzb;
@@ -410,6 +428,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     } while (0)
     CKC(ose::configure_kernels());
     CKC(ose::configure_plane_kernels());
+    CKC(ose::configure_tensor_kernels());
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
@@ -553,7 +572,7 @@ ose_status ose_step(ose_handle* h)
     CK(h, enqueue_step(h, nullptr));
     CK(h, cudaStreamSynchronize(h->stream));
     h->it += 1;
-    return OSE_OK;
+    return tensor_status(h);
 }
 
 static ose_status run_graph(ose_handle* h, int nsteps)
@@ -573,6 +592,7 @@ ose_status ose_run(ose_handle* h, int nsteps, float* gather_out)
     if (s != OSE_OK) return s;
     CK(h, cudaStreamSynchronize(h->stream));
     h->it += nsteps;
+    if ((s = tensor_status(h)) != OSE_OK) return s;
     if (gather_out) return ose_get_gather(h, gather_out);
     return OSE_OK;
 }
@@ -590,7 +610,7 @@ ose_status ose_run_record(ose_handle* h, int nsteps, float* rows_out)
         CK(h, cudaStreamSynchronize(h->stream));
         h->it += 1;
     }
-    return OSE_OK;
+    return tensor_status(h);
 }
 
 ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms)
@@ -607,7 +627,7 @@ ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms)
     CK(h, cudaEventSynchronize(h->ev1));
     CK(h, cudaEventElapsedTime(ms, h->ev0, h->ev1));
     h->it += nsteps;
-    return OSE_OK;
+    return tensor_status(h);
 }
 
 ose_status ose_select_path(ose_handle* h, int path)
@@ -619,6 +639,38 @@ ose_status ose_select_path(ose_handle* h, int path)
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     h->d.path = path;
+    return OSE_OK;
+}
+
+ose_status ose_set_precision(ose_handle* h, int mode)
+{
+    if (!h) return OSE_ERR_INVALID;
+    if (mode < OSE_PRECISION_FP32 || mode > OSE_PRECISION_BF16X3) return fail(h, OSE_ERR_INVALID, "unknown precision mode");
+    if (mode != OSE_PRECISION_FP32 && !ose::tensor_zpass_supported(h->d.nxb, h->d.nyb, h->d.nzb))
+        return fail(h, OSE_ERR_UNSUPPORTED, "the tensor-core z pass needs nzb = 256 and nxb a multiple of 16");
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (mode != OSE_PRECISION_FP32) {
+        if (!h->tcb) {
+            CK(h, dalloc(h, (uint8_t**)&h->tcb, ose::tensor_operand_bytes(OSE_PRECISION_TF32)));
+            CK(h, dalloc(h, &h->tcerr, 1));
+            CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
+        }
+        std::vector<uint8_t> ops;
+        ose::tensor_operands(mode, ops);
+        CK(h, cudaMemcpy(h->tcb, ops.data(), ops.size(), cudaMemcpyHostToDevice));
+    }
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    h->precision = mode;
+    h->tables.tcvar = mode;
+    h->tables.tcb = h->tcb;
+    h->tables.tcerr = h->tcerr;
+    return OSE_OK;
+}
+
+ose_status ose_get_precision(const ose_handle* h, int* mode)
+{
+    if (!h || !mode) return OSE_ERR_INVALID;
+    *mode = h->precision;
     return OSE_OK;
 }
 
@@ -709,7 +761,7 @@ ose_status ose_apply_operator(ose_handle* h, const float* in, float* out)
                                          h->sch, h->scl));
     CK(h, cudaMemcpyAsync(out, h->S, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    return OSE_OK;
+    return tensor_status(h);
 }
 
 ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const char** names,

@@ -62,6 +62,11 @@ struct Tables {
     const float* kx2l;    // plane path: low parts of the squared wavenumbers
     const float* ky2l;
     const float* kz2l;
+    // precision form (ose_tensor.cu): OSE_PRECISION_* of the z pass, its DFT
+    // operands in shared-memory layout and the device error word
+    int tcvar;
+    const void* tcb;
+    int* tcerr;
 };
 
 // Compensated constants: when true, the Bessel coefficients, 1/(R N) and |k|
@@ -103,6 +108,13 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
 cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
                                         const float* vs, float sch, float scl, const Tables& t);
 int plane_max_active_clusters();
+
+// Precision form: tensor-core z pass (ose_tensor.cu).
+bool tensor_zpass_supported(int nxb, int nyb, int nzb);
+size_t tensor_operand_bytes(int var);
+void tensor_operands(int var, std::vector<uint8_t>& out);
+cudaError_t configure_tensor_kernels();
+cudaError_t launch_tensor_zpass(cudaStream_t s, float2* X, const Geometry& g, const Tables& t);
 
 // ---- batched shots (ose_batch.cu host side, kernels in ose_kernels.cu) ----
 constexpr int kMaxTerms = 48;   // series terms M + 1 a batched shot may use

@@ -338,10 +338,15 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     }
     {
         Timer T(tm, s, T_ZK);
-        const int tx = tile_x(pz.n);
-        dim3 grid((g.nxb + tx - 1) / tx, g.nyb);
-        k_lines<false, true><<<grid, kThreads, lines_smem(pz.n), s>>>(X, g, pz, t.twz, tx,
-                                                                     (long long)g.nxb * g.nyb, t);
+        if (t.tcvar != OSE_PRECISION_FP32) {
+            cudaError_t e = launch_tensor_zpass(s, X, g, t);
+            if (e != cudaSuccess) return e;
+        } else {
+            const int tx = tile_x(pz.n);
+            dim3 grid((g.nxb + tx - 1) / tx, g.nyb);
+            k_lines<false, true><<<grid, kThreads, lines_smem(pz.n), s>>>(X, g, pz, t.twz, tx,
+                                                                         (long long)g.nxb * g.nyb, t);
+        }
         T.done();
     }
     {

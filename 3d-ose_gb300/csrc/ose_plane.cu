@@ -572,6 +572,10 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
 
 cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
 {
+    if (t.tcvar != OSE_PRECISION_FP32) {
+        Geometry g{plane::N, plane::N, plane::N, (long long)plane::N * plane::N * plane::N};
+        return launch_tensor_zpass(s, X, g, t);
+    }
     plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(X, t.twx, t);
     return cudaGetLastError();
 }

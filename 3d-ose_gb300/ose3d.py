@@ -21,6 +21,9 @@ FIELD_P, FIELD_Q, FIELD_V = 0, 1, 2
 LAYOUT_ZYX, LAYOUT_YXZ = 0, 1
 SPONGE_REFERENCE, SPONGE_CERJAN = 0, 1
 PATH_GENERIC, PATH_PLANE = 0, 1
+PRECISION_FP32, PRECISION_TF32, PRECISION_TF32X3, PRECISION_BF16X3 = 0, 1, 2, 3
+PRECISIONS = {"fp32": PRECISION_FP32, "tf32": PRECISION_TF32, "tf32x3": PRECISION_TF32X3,
+              "bf16x3": PRECISION_BF16X3}
 NOALLOC_MAX_CELLS = 262144   # OSE_NOALLOC_MAX_CELLS
 
 STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOMEM",
@@ -36,7 +39,7 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_write_segy", "ose_batch_create", "ose_batch_destroy", "ose_batch_last_error",
            "ose_batch_reset", "ose_batch_run", "ose_batch_run_timed", "ose_batch_info",
            "ose_batch_get_gather", "ose_batch_get_wavefield", "ose_batch_autotune",
-           "ose_batch_get_tuning"]
+           "ose_batch_get_tuning", "ose_set_precision", "ose_get_precision"]
 
 # void (*)(int it, const float* P, const float* Q, void* user)
 SNAPSHOT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
@@ -112,6 +115,8 @@ def load_library(path: str = LIB_PATH):
         "ose_run_record": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_run_timed": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_select_path": ([H, ctypes.c_int], ctypes.c_int),
+        "ose_set_precision": ([H, ctypes.c_int], ctypes.c_int),
+        "ose_get_precision": ([H, P(ctypes.c_int)], ctypes.c_int),
         "ose_get_it": ([H, P(ctypes.c_int)], ctypes.c_int),
         "ose_get_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
         "ose_set_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
@@ -342,6 +347,21 @@ class Modeler:
         """PATH_PLANE (256^3 only) or PATH_GENERIC."""
         self._check(self._lib.ose_select_path(self._h, path))
         self._check(self._lib.ose_get_derived(self._h, ctypes.byref(self.derived)))
+
+    @property
+    def precision(self) -> int:
+        """Arithmetic of the z-axis transforms (PRECISION_*)."""
+        v = ctypes.c_int()
+        self._check(self._lib.ose_get_precision(self._h, ctypes.byref(v)))
+        return v.value
+
+    @precision.setter
+    def precision(self, mode):
+        """PRECISION_FP32 (FFT kernels) or a tensor-core DFT-matmul z pass:
+        PRECISION_TF32, PRECISION_TF32X3, PRECISION_BF16X3 (or their names)."""
+        if isinstance(mode, str):
+            mode = PRECISIONS[mode]
+        self._check(self._lib.ose_set_precision(self._h, int(mode)))
 
     @property
     def it(self) -> int:

@@ -54,6 +54,12 @@ CONFIGS = {
                        dict(nx=260, ny=228, nz=196, bu=30, bd=30, bl=30, br=30, bf=30, bb=30,
                             nt=2000, fm=25.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
                             sxbeg=130, sybeg=114, szbeg=5, gzbeg=0)),
+    # Precision-form workload: padded 384 x 384 x 256 = interior 324 x 324 x 196
+    # + 30-cell sponge, same velocity generator, 15 Hz Ricker, 1500 steps.
+    "ose384x384x256": (lambda: smooth_random_salt(324, 324, 196, seed=2026),
+                       dict(nx=324, ny=324, nz=196, bu=30, bd=30, bl=30, br=30, bf=30, bb=30,
+                            nt=1500, fm=15.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                            sxbeg=162, sybeg=162, szbeg=5, gzbeg=0)),
     # Interior 101^3 + 20-cell sponge (padded 142^3), 20 Hz at (50,50,10), 1000 steps,
     # receivers at z = 5.
     "ose142": (lambda: layered_perturbed(101, 101, 101),

@@ -236,6 +236,54 @@ def run_batched(args, rank):
     return 0
 
 
+def run_precision(args, rank):
+    """--workload precision: the precision form.  For each z-pass arithmetic
+    (FP32 FFT kernels; TF32, TF32X3, BF16X3 tensor-core DFT matmuls) the step
+    rate on the padded 384 x 384 x 256 workload (15 Hz, 1500 steps) and on the
+    256^3 workload, and the z-pass kernel's HBM rate and tensor FLOP rate
+    (per cell per z pass: 4 DFT-16 matmul stages x 128 flop x products)."""
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+    ge.build_library()
+    import ose3d
+    import workloads
+
+    peak, peak_kind = measured_peak_hbm()
+    K = max(1, min(args.steps, 100))
+    out = {}
+    for wl in ("ose384x384x256", "ose256"):
+        build, kw = workloads.CONFIGS[wl]
+        vel = build()
+        res = {}
+        with ose3d.Modeler(ose3d.default_params(**kw), vel) as m:
+            d = m.derived
+            cells = d.nxb * d.nyb * d.nzb
+            for name, mode in ose3d.PRECISIONS.items():
+                m.precision = mode
+                m.reset_shot(0)
+                m.run(max(3, args.warmup))
+                ms = m.run_timed(K)
+                rows, _ = m.profile_step(reps=2)
+                z = [r for r in rows if r["name"] in ("fft_z_kscale", "zpass")][0]
+                prods = {"fp32": 0, "tf32": 1, "tf32x3": 3, "bf16x3": 3}[name]
+                res[name] = {"gcell_steps_s": cells * K / (ms * 1e-3) / 1e9, "ms_per_step": ms / K,
+                             "zpass_ms": z["ms"], "zpass_gbs": z["bytes"] / (z["ms"] * 1e-3) / 1e9,
+                             "zpass_hbm_frac": z["bytes"] / (z["ms"] * 1e-3) / 1e9 / peak,
+                             "zpass_tensor_tflops": 512.0 * prods * cells / (z["ms"] * 1e-3) / 1e12}
+            out[wl] = {"grid": [d.nxb, d.nyb, d.nzb], "M": d.M,
+                       "kernel_path": "generic" if d.path == 0 else "plane", "variants": res}
+    base = out["ose384x384x256"]["variants"]
+    line = {"metric": "Gcell-steps/s of the precision form (tensor-core z pass) vs the FP32 FFT z pass",
+            "value": base["tf32x3"]["gcell_steps_s"], "unit": UNIT, "n_gpus": 1, "steps": K,
+            "warmup": max(3, args.warmup), "ms_per_step": base["tf32x3"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3",
+            "data": DATA, "config": {"workload": "precision", "peak_hbm_gbs": peak,
+                                     "peak_source": peak_kind, "results": out}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -243,7 +291,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched64"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched64", "precision"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -251,6 +299,8 @@ def main():
     if args.workload == "batched64":
         import numpy as np  # noqa: F401
         return run_batched(args, rank)
+    if args.workload == "precision":
+        return run_precision(args, rank)
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     dist = Dist(world)

@@ -165,6 +165,22 @@ ose_status ose_run_timed(ose_handle* h, int nsteps, float* ms);
  * step; the choice exists for comparison and testing. */
 ose_status ose_select_path(ose_handle* h, int path);
 
+/* Arithmetic of the z-axis transforms (the precision form; no counterpart in
+ * the reference, whose transforms are cuFFT FP32).  FP32 is the FFT kernels.
+ * The others run the z pass (FFT_z, * |k|, IFFT_z) as four batched DFT-16
+ * matmuls on the tensor cores with FP32 accumulation: TF32 one pass; TF32X3
+ * and BF16X3 split each operand into hi + lo parts and add the three products
+ * lo*hi + hi*lo + hi*hi.  Needs nzb = 256 and nxb a multiple of 16
+ * (OSE_ERR_UNSUPPORTED otherwise); works with either path. */
+enum {
+    OSE_PRECISION_FP32 = 0,
+    OSE_PRECISION_TF32 = 1,
+    OSE_PRECISION_TF32X3 = 2,
+    OSE_PRECISION_BF16X3 = 3
+};
+ose_status ose_set_precision(ose_handle* h, int mode);
+ose_status ose_get_precision(const ose_handle* h, int* mode);
+
 /* Steps taken in the current shot. */
 ose_status ose_get_it(const ose_handle* h, int* it);
 
