@@ -13,6 +13,7 @@
 
 #include "ose_internal.h"
 #include "ose_io.h"
+#include "ose_learn.h"
 
 using ose::AxisPlan;
 
@@ -47,6 +48,9 @@ struct ose_handle {
     int precision = OSE_PRECISION_FP32;
     void* tcb = nullptr;
     int* tcerr = nullptr;
+    // learned boundary corrector (inference buffers) and the velocity it reads
+    ose_corrector* corr = nullptr;
+    float* corr_vel = nullptr;
 
     // host copies
     std::vector<float> vb, h_ax, h_ay, h_az, h_ricker, h_hil;
@@ -125,6 +129,8 @@ void free_all(ose_handle* h)
     }
     if (h->snap_ready) cudaEventDestroy(h->snap_ready);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->corr) ose::learn::delete_corrector(h->corr);
+    if (h->corr_vel) cudaFree(h->corr_vel);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -145,6 +151,16 @@ cudaError_t timed(ose::KernelTiming* tm, cudaStream_t s, int cls, double bytes, 
         tm->bytes[cls] += bytes;
     }
     return e;
+}
+
+// The learned boundary correction at the end of a step (timing class 6;
+// bytes: the shell's features, three hidden layers and the state update).
+cudaError_t enqueue_corrector(ose_handle* h, ose::KernelTiming* tm)
+{
+    if (!h->corr) return cudaSuccess;
+    const ose::learn::Net& n = ose::learn::net_of(h->corr);
+    const double bytes = (double)n.ncells * (8.0 + 8 * 4 + 3 * 2 * 32 * 4 + 8.0);
+    return timed(tm, h->stream, 6, bytes, [&] { return ose::learn::forward(h->stream, n, h->W, h->corr_vel, true, h->W); });
 }
 
 // Plane path step: 2 HBM passes per operator application (ose_plane.cu).
@@ -203,7 +219,7 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
         e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->tables, ea); });
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return enqueue_corrector(h, tm);
 }
 
 // Enqueue one whole time step on h->stream (no synchronisation).
@@ -252,7 +268,7 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
         if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += (n == M ? 36.0 : 44.0) * N; }
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return enqueue_corrector(h, tm);
 }
 
 ose_status build_graph(ose_handle* h)
@@ -674,6 +690,67 @@ ose_status ose_get_precision(const ose_handle* h, int* mode)
     return OSE_OK;
 }
 
+ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
+{
+    if (!h) return OSE_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    if (h->corr) { ose::learn::delete_corrector(h->corr); h->corr = nullptr; }
+    if (!params) return OSE_OK;
+    const int sp[6] = {h->p.bl, h->d.br, h->p.bf, h->d.bb, h->p.bu, h->d.bd};
+    for (int i = 0; i < 6; ++i)
+        if (shell < 1 || sp[i] > shell) return fail(h, OSE_ERR_INVALID, "the shell must be at least as wide as every sponge");
+    ose::learn::NetGeom g{h->d.nxb, h->d.nyb, h->d.nzb, shell, {sp[0], sp[1], sp[2], sp[3], sp[4], sp[5]}};
+    h->corr = ose::learn::new_corrector();
+    cudaError_t e = ose::learn::create_net(h->corr, g, false);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(ose::learn::net_of(h->corr).params, params, sizeof(float) * ose::learn::param_count(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !h->corr_vel) {
+        e = cudaMalloc((void**)&h->corr_vel, sizeof(float) * h->vb.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->corr_vel, h->vb.data(), sizeof(float) * h->vb.size(), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        ose::learn::delete_corrector(h->corr);
+        h->corr = nullptr;
+        return cuda_fail(h, e, "ose_set_corrector");
+    }
+    return OSE_OK;
+}
+
+namespace {
+__global__ void k_box(const float2* __restrict__ src, int snx, int sny, int sx0, int sy0, int sz0,
+                      float2* __restrict__ dst, int dnx, int dny, int dx0, int dy0, int dz0, int nx, int ny, int nz)
+{
+    const long long n = (long long)nx * ny * nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));
+        dst[((size_t)(z + dz0) * dny + (y + dy0)) * dnx + (x + dx0)] =
+            src[((size_t)(z + sz0) * sny + (y + sy0)) * snx + (x + sx0)];
+    }
+}
+}  // namespace
+
+ose_status ose_state_box(ose_handle* h, int dir, const int* box, void* buf_dev, const int* buf)
+{
+    if (!h || !box || !buf || !buf_dev || (dir != 0 && dir != 1)) return OSE_ERR_INVALID;
+    const int x0 = box[0], y0 = box[1], z0 = box[2], nx = box[3], ny = box[4], nz = box[5];
+    const int bnx = buf[0], bny = buf[1], bx0 = buf[2], by0 = buf[3], bz0 = buf[4];
+    if (nx < 1 || ny < 1 || nz < 1 || x0 < 0 || y0 < 0 || z0 < 0 || x0 + nx > h->d.nxb || y0 + ny > h->d.nyb ||
+        z0 + nz > h->d.nzb || bx0 < 0 || by0 < 0 || bz0 < 0 || bx0 + nx > bnx || by0 + ny > bny)
+        return fail(h, OSE_ERR_INVALID, "box outside the grid or the buffer");
+    float2* b = static_cast<float2*>(buf_dev);
+    const unsigned blocks = (unsigned)std::min<long long>(4096, ((long long)nx * ny * nz + 255) / 256);
+    if (dir == 0)
+        k_box<<<blocks, 256, 0, h->stream>>>(h->W, h->d.nxb, h->d.nyb, x0, y0, z0, b, bnx, bny, bx0, by0, bz0, nx, ny, nz);
+    else
+        k_box<<<blocks, 256, 0, h->stream>>>(b, bnx, bny, bx0, by0, bz0, h->W, h->d.nxb, h->d.nyb, x0, y0, z0, nx, ny, nz);
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
+    return OSE_OK;
+}
+
 ose_status ose_get_it(const ose_handle* h, int* it)
 {
     if (!h || !it) return OSE_ERR_INVALID;
@@ -772,11 +849,11 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
     if (h->it + reps > h->p.nt) return fail(h, OSE_ERR_INVALID, "reps beyond nt");
     ose::KernelTiming& t = h->timing;
     static const char* kGeneric[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
-                                     "fft_x_inv_epilogue", "inject"};
+                                     "fft_x_inv_epilogue", "inject", "corrector"};
     static const char* kPlane[] = {"plane_fwd", "zpass", "plane_inv_first", "plane_inv_mid",
-                                   "plane_inv_last", "inject"};
+                                   "plane_inv_last", "inject", "corrector"};
     const char** kNames = h->d.path == OSE_PATH_PLANE ? kPlane : kGeneric;
-    const int nc = 6;
+    const int nc = h->corr ? 7 : 6;
     for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
     for (int r = 0; r < reps; ++r) {
         CK(h, enqueue_step(h, &t));

@@ -1,0 +1,66 @@
+// ose_learn.h - the learned-boundary corrector (ose_learn.cu): geometry,
+// device buffers and launch helpers shared with the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/ose3d.h"
+
+namespace ose {
+namespace learn {
+
+constexpr int kLayers = 4;
+extern const int kCin[kLayers];
+extern const int kCout[kLayers];
+
+// Padded grid, shell width and sponge widths (x-, x+, y-, y+, z-, z+).
+struct NetGeom {
+    int nx, ny, nz;
+    int shell;
+    int sp[6];
+};
+
+// One network instance on one grid: parameters and every work buffer
+// (device pointers; dense over the padded grid, channels last).
+struct Net {
+    NetGeom g;
+    int* tiles;            // 8^3 tiles meeting the shell, packed i | j << 10 | k << 20
+    int ntiles;
+    long long ncells;      // shell cells
+    long long nwrite;      // write cells (shell outside the sponge)
+    float* params;         // param_count() floats
+    float* grads;
+    float* m;
+    float* v;
+    float* wt[kLayers];    // data-gradient weights of layers 1..3
+    float* F;              // [cell][8] input features
+    float* A[3];           // [cell][32] hidden activations
+    float* O;              // [cell][2] output
+    float* G4;             // [cell][2] output gradient
+    float* GA[3];          // [cell][32] gradients of the hidden activations
+    float* scal;           // [0] sum of squares, [1] s, [2] 1/s
+    float* loss;           // [0] accumulated loss
+};
+
+size_t param_offset(int layer);
+size_t param_count();
+void shell_tiles(const NetGeom& g, std::vector<int>& tiles, long long* ncells, long long* nwrite);
+cudaError_t configure();
+// Forward pass on state W (float2 P + iQ, [z][y][x]) and velocity vel.  With
+// apply, adds the correction to state_out (may equal W); else writes n.O.
+cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out);
+// Forward + backward of one sample; gradients add into n.grads, loss into n.loss.
+cudaError_t train_sample(cudaStream_t s, const Net& n, const float2* W, const float* vel, const float2* tgt);
+// One Adam update with gradients scaled by gscale; clears the gradients.
+cudaError_t adam(cudaStream_t s, const Net& n, float lr, float b1, float b2, float eps, int step, float gscale);
+
+// Corrector objects (the C ABI's ose_corrector) for the modeler's own use.
+ose_corrector* new_corrector();
+void delete_corrector(ose_corrector* c);
+cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training);
+const Net& net_of(const ose_corrector* c);
+
+}  // namespace learn
+}  // namespace ose

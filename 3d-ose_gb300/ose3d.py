@@ -39,7 +39,12 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_write_segy", "ose_batch_create", "ose_batch_destroy", "ose_batch_last_error",
            "ose_batch_reset", "ose_batch_run", "ose_batch_run_timed", "ose_batch_info",
            "ose_batch_get_gather", "ose_batch_get_wavefield", "ose_batch_autotune",
-           "ose_batch_get_tuning", "ose_set_precision", "ose_get_precision"]
+           "ose_batch_get_tuning", "ose_set_precision", "ose_get_precision", "ose_set_corrector",
+           "ose_state_box", "ose_corrector_param_count", "ose_corrector_create", "ose_corrector_destroy",
+           "ose_corrector_last_error", "ose_corrector_info", "ose_corrector_set_params",
+           "ose_corrector_get_params", "ose_corrector_get_grads", "ose_corrector_forward",
+           "ose_corrector_apply", "ose_corrector_train_sample", "ose_corrector_adam", "ose_corrector_loss"]
+CORRECTOR_SHELL = 16   # OSE_CORRECTOR_SHELL
 
 # void (*)(int it, const float* P, const float* Q, void* user)
 SNAPSHOT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
@@ -116,6 +121,22 @@ def load_library(path: str = LIB_PATH):
         "ose_run_timed": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_select_path": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_precision": ([H, ctypes.c_int], ctypes.c_int),
+        "ose_set_corrector": ([H, f32, ctypes.c_int], ctypes.c_int),
+        "ose_state_box": ([H, ctypes.c_int, P(ctypes.c_int), ctypes.c_void_p, P(ctypes.c_int)], ctypes.c_int),
+        "ose_corrector_param_count": ([], ctypes.c_size_t),
+        "ose_corrector_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), P(H)],
+                                 ctypes.c_int),
+        "ose_corrector_destroy": ([H], ctypes.c_int),
+        "ose_corrector_last_error": ([H], ctypes.c_char_p),
+        "ose_corrector_info": ([H, P(ctypes.c_longlong), P(ctypes.c_longlong), P(ctypes.c_int)], ctypes.c_int),
+        "ose_corrector_set_params": ([H, f32], ctypes.c_int),
+        "ose_corrector_get_params": ([H, f32], ctypes.c_int),
+        "ose_corrector_get_grads": ([H, f32], ctypes.c_int),
+        "ose_corrector_forward": ([H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, f32], ctypes.c_int),
+        "ose_corrector_apply": ([H, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "ose_corrector_train_sample": ([H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "ose_corrector_adam": ([H, ctypes.c_float, ctypes.c_int, f32], ctypes.c_int),
+        "ose_corrector_loss": ([H, f32, ctypes.c_int], ctypes.c_int),
         "ose_get_precision": ([H, P(ctypes.c_int)], ctypes.c_int),
         "ose_get_it": ([H, P(ctypes.c_int)], ctypes.c_int),
         "ose_get_wavefield": ([H, ctypes.c_int, f32, ctypes.c_int], ctypes.c_int),
@@ -188,6 +209,90 @@ class ShotWindow(ctypes.Structure):
     """ose_shot_window (include/ose3d.h)."""
 
     _fields_ = [(k, ctypes.c_int) for k in ("x0", "y0", "z0", "nx", "ny", "nz", "sx", "sy", "sz")]
+
+
+class Corrector:
+    """Training object of the learned boundary corrector on one padded grid
+    (ose_corrector_*).  Device buffers are passed as integer device pointers
+    (e.g. torch's tensor.data_ptr()); work runs on the default stream."""
+
+    def __init__(self, shape_zyx, sponge6, shell: int = CORRECTOR_SHELL):
+        self._lib = load_library()
+        nz, ny, nx = shape_zyx
+        h = ctypes.c_void_p()
+        sp = (ctypes.c_int * 6)(*[int(v) for v in sponge6])
+        rc = self._lib.ose_corrector_create(nx, ny, nz, shell, sp, ctypes.byref(h))
+        if rc != OK:
+            raise OseError(rc, self._lib.ose_corrector_last_error(None).decode())
+        self._h = h
+        self.shape = tuple(shape_zyx)
+        self.nparams = int(self._lib.ose_corrector_param_count())
+
+    def _check(self, rc):
+        if rc != OK:
+            raise OseError(rc, self._lib.ose_corrector_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ose_corrector_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        sc, wc, nt = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+        self._check(self._lib.ose_corrector_info(self._h, ctypes.byref(sc), ctypes.byref(wc), ctypes.byref(nt)))
+        return dict(shell_cells=sc.value, write_cells=wc.value, tiles=nt.value)
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.nparams
+        self._check(self._lib.ose_corrector_set_params(self._h, _f32(p)))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.nparams, np.float32)
+        self._check(self._lib.ose_corrector_get_params(self._h, _f32(p)))
+        return p
+
+    def grads(self) -> np.ndarray:
+        g = np.zeros(self.nparams, np.float32)
+        self._check(self._lib.ose_corrector_get_grads(self._h, _f32(g)))
+        return g
+
+    def forward(self, state_ptr: int, vel_ptr: int, out_ptr: int | None = None) -> float:
+        s = ctypes.c_float()
+        self._check(self._lib.ose_corrector_forward(self._h, state_ptr, vel_ptr, out_ptr, ctypes.byref(s)))
+        return s.value
+
+    def apply(self, state_ptr: int, vel_ptr: int):
+        self._check(self._lib.ose_corrector_apply(self._h, state_ptr, vel_ptr))
+
+    def train_sample(self, state_ptr: int, vel_ptr: int, target_ptr: int):
+        self._check(self._lib.ose_corrector_train_sample(self._h, state_ptr, vel_ptr, target_ptr))
+
+    def adam(self, lr: float, batch: int) -> float:
+        l = ctypes.c_float()
+        self._check(self._lib.ose_corrector_adam(self._h, lr, batch, ctypes.byref(l)))
+        return l.value
+
+    def loss(self, reset: bool = False) -> float:
+        l = ctypes.c_float()
+        self._check(self._lib.ose_corrector_loss(self._h, ctypes.byref(l), int(reset)))
+        return l.value
+
+
+def corrector_param_count() -> int:
+    return int(load_library().ose_corrector_param_count())
 
 
 class Batch:
@@ -397,6 +502,21 @@ class Modeler:
         ax, ay, az = (np.zeros(n, np.float32) for n in (d.nxb, d.nyb, d.nzb))
         self._check(self._lib.ose_get_sponge(self._h, _f32(ax), _f32(ay), _f32(az)))
         return ax, ay, az
+
+    def set_corrector(self, params: np.ndarray | None, shell: int = CORRECTOR_SHELL):
+        """Attach a trained learned-boundary corrector (None detaches)."""
+        if params is None:
+            self._check(self._lib.ose_set_corrector(self._h, None, shell))
+            return
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self._lib.ose_set_corrector(self._h, _f32(p), shell))
+
+    def state_box(self, direction: int, box, buf_ptr: int, buf):
+        """Copy a box of the state to (direction 0) or from (1) a device
+        buffer: box = (x0, y0, z0, nx, ny, nz), buf = (bnx, bny, bx0, by0, bz0)."""
+        b = (ctypes.c_int * 6)(*[int(v) for v in box])
+        f = (ctypes.c_int * 5)(*[int(v) for v in buf])
+        self._check(self._lib.ose_state_box(self._h, direction, b, buf_ptr, f))
 
     def apply_operator(self, x: np.ndarray) -> np.ndarray:
         """v * IFFT3(|k| FFT3(x)) / (R N) on a complex64 [nzb][nyb][nxb] field."""

@@ -181,6 +181,58 @@ enum {
 ose_status ose_set_precision(ose_handle* h, int mode);
 ose_status ose_get_precision(const ose_handle* h, int* mode);
 
+/* ---- learned boundary corrector (no counterpart in the reference) --------
+ * A 3D convolutional network (4 layers of 3x3x3 convolutions, 8 -> 32 -> 32
+ * -> 32 -> 2 channels, ReLU, ose_corrector_param_count() FP32 parameters)
+ * that runs on the SHELL of the padded grid (cells within `shell` cells of a
+ * face; the grid is periodic) and adds a correction to P and Q at the shell
+ * cells outside the sponge, so that a thin sponge behaves like a wide one.
+ * Inputs per cell: P/s, Q/s (s = RMS of P, Q over the shell), v/4500 and the
+ * signed closeness to the nearest face of each axis.  Parameter layout: per
+ * layer W[27][Cin][Cout] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)) then b[Cout];
+ * layer 0 has Cin = 8 (channels 6, 7 are zero). */
+#define OSE_CORRECTOR_SHELL 16
+typedef struct ose_corrector ose_corrector;
+
+/* Attach a trained corrector to a modeler (params: host, param_count floats;
+ * NULL detaches).  Every time step then ends with the correction, inside the
+ * captured graph.  The receiver row of a step is recorded before it. */
+ose_status ose_set_corrector(ose_handle* h, const float* params, int shell);
+
+/* Copy a box of the state (P + iQ as float pairs, [z][y][x]) to or from a
+ * caller-owned DEVICE buffer: dir 0 state -> buffer, 1 buffer -> state.
+ * box = {x0, y0, z0, nx, ny, nz} in the padded grid; buf = {bnx, bny, bx0,
+ * by0, bz0}: the buffer's x and y sizes and the box's origin in it.  For
+ * pipelines that pair two modelers on the device (training data). */
+ose_status ose_state_box(ose_handle* h, int dir, const int* box, void* buf_dev, const int* buf);
+
+/* Training objects: every call takes device pointers (state and target as
+ * float pairs [z][y][x] on the corrector's grid, velocity as floats) and runs
+ * on the legacy default stream, ordered with the caller's default-stream work. */
+size_t ose_corrector_param_count(void);
+ose_status ose_corrector_create(int nxb, int nyb, int nzb, int shell, const int* sponge6, ose_corrector** out);
+ose_status ose_corrector_destroy(ose_corrector* c);
+const char* ose_corrector_last_error(const ose_corrector* c);
+ose_status ose_corrector_info(const ose_corrector* c, long long* shell_cells, long long* write_cells, int* tiles);
+ose_status ose_corrector_set_params(ose_corrector* c, const float* params);
+ose_status ose_corrector_get_params(ose_corrector* c, float* params);
+ose_status ose_corrector_get_grads(ose_corrector* c, float* grads);
+/* Network output (dP, dQ)/s per cell ([cell][2] floats, written at shell
+ * cells) and the scale s. */
+ose_status ose_corrector_forward(ose_corrector* c, const void* state_dev, const float* vel_dev, float* out_dev,
+                                 float* scale_out);
+/* state += s * output at the write cells (what a modeler's step does). */
+ose_status ose_corrector_apply(ose_corrector* c, void* state_dev, const float* vel_dev);
+/* Forward + backward of one sample: loss = mean over write cells of
+ * |output - (target - state)/s|^2; gradients and loss accumulate. */
+ose_status ose_corrector_train_sample(ose_corrector* c, const void* state_dev, const float* vel_dev,
+                                      const void* target_dev);
+/* Adam step (beta 0.9, 0.999) on the gradients accumulated over `batch`
+ * samples, which it clears; *mean_loss = their mean loss. */
+ose_status ose_corrector_adam(ose_corrector* c, float lr, int batch, float* mean_loss);
+/* Accumulated loss; reset != 0 also clears it and the gradients. */
+ose_status ose_corrector_loss(ose_corrector* c, float* loss, int reset);
+
 /* Steps taken in the current shot. */
 ose_status ose_get_it(const ose_handle* h, int* it);
 

@@ -71,3 +71,8 @@ def test_python_class_mirrors_header_structs():
     assert ctypes.sizeof(ose3d.Params) == ctypes.sizeof(O.OseParams)
     assert [f[0] for f in ose3d.Params._fields_] == [f[0] for f in O.OseParams._fields_]
     assert [f[0] for f in ose3d.Derived._fields_] == [f[0] for f in O.OseDerived._fields_]
+
+
+def test_corrector_param_count_matches_the_restatement(lib):
+    import corrector_torch as CT
+    assert ose3d.corrector_param_count() == CT.param_count() == 64034
