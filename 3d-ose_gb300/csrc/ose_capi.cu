@@ -159,8 +159,15 @@ cudaError_t enqueue_corrector(ose_handle* h, ose::KernelTiming* tm)
 {
     if (!h->corr) return cudaSuccess;
     const ose::learn::Net& n = ose::learn::net_of(h->corr);
-    const double bytes = (double)n.ncells * (8.0 + 8 * 4 + 3 * 2 * 32 * 4 + 8.0);
-    return timed(tm, h->stream, 6, bytes, [&] { return ose::learn::forward(h->stream, n, h->W, h->corr_vel, true, h->W); });
+    const ose::learn::TcNet* tc = ose::learn::tc_of(h->corr);
+    // shell bytes: scale read, layer 0 reads state + velocity and writes 32
+    // BF16 channels, two hidden layers read and write them, the output layer
+    // reads them and updates the state
+    const double bytes = (double)n.ncells * (8.0 + 12.0 + 64.0 + 2 * 128.0 + 64.0 + 16.0);
+    return timed(tm, h->stream, 6, bytes, [&] {
+        return tc ? ose::learn::forward_tc(h->stream, n, *tc, h->W, h->corr_vel)
+                  : ose::learn::forward(h->stream, n, h->W, h->corr_vel, true, h->W);
+    });
 }
 
 // Plane path step: 2 HBM passes per operator application (ose_plane.cu).
@@ -292,12 +299,13 @@ ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVAL
 // of time in its error word (the kernel then leaves its columns unchanged).
 ose_status tensor_status(ose_handle* h)
 {
-    if (h->precision == OSE_PRECISION_FP32 || !h->tcerr) return OSE_OK;
+    if ((h->precision == OSE_PRECISION_FP32 && !h->corr) || !h->tcerr) return OSE_OK;
     int v = 0;
     CK(h, cudaMemcpy(&v, h->tcerr, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
         CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
-        return fail(h, OSE_ERR_CUDA, "tensor-core z pass: an MMA completion wait ran out of time");
+        return fail(h, OSE_ERR_CUDA, v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
+                                            : "tensor-core z pass: an MMA completion wait ran out of time");
     }
     return OSE_OK;
 }
@@ -666,8 +674,8 @@ ose_status ose_set_precision(ose_handle* h, int mode)
         return fail(h, OSE_ERR_UNSUPPORTED, "the tensor-core z pass needs nzb = 256 and nxb a multiple of 16");
     CK(h, cudaStreamSynchronize(h->stream));
     if (mode != OSE_PRECISION_FP32) {
-        if (!h->tcb) {
-            CK(h, dalloc(h, (uint8_t**)&h->tcb, ose::tensor_operand_bytes(OSE_PRECISION_TF32)));
+        if (!h->tcb) CK(h, dalloc(h, (uint8_t**)&h->tcb, ose::tensor_operand_bytes(OSE_PRECISION_TF32)));
+        if (!h->tcerr) {
             CK(h, dalloc(h, &h->tcerr, 1));
             CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
         }
@@ -711,6 +719,13 @@ ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
         if (e == cudaSuccess)
             e = cudaMemcpy(h->corr_vel, h->vb.data(), sizeof(float) * h->vb.size(), cudaMemcpyHostToDevice);
     }
+    if (e == cudaSuccess && !h->tcerr) {
+        e = cudaMalloc((void**)&h->tcerr, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(h->tcerr, 0, sizeof(int));
+    }
+    // the tensor-core kernels unless OSE3D_CORRECTOR=fp32 asks for the FP32 ones
+    const char* mode = getenv("OSE3D_CORRECTOR");
+    if (e == cudaSuccess && !(mode && strcmp(mode, "fp32") == 0)) e = ose::learn::create_tc(h->corr, params, h->tcerr);
     if (e != cudaSuccess) {
         ose::learn::delete_corrector(h->corr);
         h->corr = nullptr;

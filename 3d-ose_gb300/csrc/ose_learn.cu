@@ -436,14 +436,22 @@ static unsigned grid_for(int ntiles, int per_sm)
     return (unsigned)std::max(1, std::min(ntiles, per_sm * sms));
 }
 
+cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
+{
+    cudaMemsetAsync(n.scal, 0, sizeof(float), s);
+    const unsigned gr = grid_for(n.ntiles, 2);
+    k_shell_sumsq<<<gr, 256, 0, s>>>(W, n.g, n.tiles, n.ntiles, n.scal);
+    k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
+    return cudaGetLastError();
+}
+
 cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out)
 {
     const NetGeom& g = n.g;
     const float* p = n.params;
-    cudaMemsetAsync(n.scal, 0, sizeof(float), s);
     const unsigned gr = grid_for(n.ntiles, 2);
-    k_shell_sumsq<<<gr, 256, 0, s>>>(W, g, n.tiles, n.ntiles, n.scal);
-    k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
+    cudaError_t e0 = shell_scale(s, n, W);
+    if (e0 != cudaSuccess) return e0;
     k_features<<<gr, 256, 0, s>>>(W, vel, n.scal, n.F, g, n.tiles, n.ntiles);
     const float* w0 = p + param_offset(0);
     const float* w1 = p + param_offset(1);
@@ -518,6 +526,8 @@ cudaError_t adam(cudaStream_t s, const Net& n, float lr, float b1, float b2, flo
 
 struct ose_corrector {
     ose::learn::Net net{};
+    ose::learn::TcNet tc{};
+    bool has_tc = false;
     std::vector<void*> bufs;
     std::string err;
     int step = 0;
@@ -587,6 +597,40 @@ cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training)
 #undef A_
     return configure();
 }
+
+cudaError_t create_tc(ose_corrector* c, const float* params_host, int* err)
+{
+    TcNet& t = c->tc;
+    std::vector<int> tiles;
+    tc_tiles(c->net.g, tiles);
+    t.ntiles = (int)tiles.size();
+    const size_t cells = (size_t)c->net.g.nx * c->net.g.ny * c->net.g.nz;
+    cudaError_t e;
+    if ((e = corr_alloc(c, &t.tiles, tiles.size(), false)) != cudaSuccess) return e;
+    if ((e = cudaMemcpy(t.tiles, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
+    const int cin_pad[kLayers] = {16, 32, 32, 32};
+    const int npad[kLayers] = {32, 32, 32, 16};
+    for (int l = 0; l < kLayers; ++l) {
+        const float* w = params_host + param_offset(l);
+        std::vector<uint8_t> wb;
+        tc_layer_weights(w, kCin[l], kCout[l], cin_pad[l], npad[l], wb);
+        std::vector<float> bb(npad[l], 0.f);
+        for (int i = 0; i < kCout[l]; ++i) bb[i] = w[(size_t)27 * kCin[l] * kCout[l] + i];
+        if ((e = corr_alloc(c, &t.w[l], wb.size(), false)) != cudaSuccess) return e;
+        if ((e = cudaMemcpy(t.w[l], wb.data(), wb.size(), cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+        if ((e = corr_alloc(c, &t.b[l], bb.size(), false)) != cudaSuccess) return e;
+        if ((e = cudaMemcpy(t.b[l], bb.data(), sizeof(float) * bb.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return e;
+    }
+    for (int i = 0; i < 2; ++i)
+        if ((e = corr_alloc(c, &t.act[i], cells * 32, false)) != cudaSuccess) return e;
+    t.err = err;
+    c->has_tc = true;
+    return configure_tc();
+}
+
+const TcNet* tc_of(const ose_corrector* c) { return c && c->has_tc ? &c->tc : nullptr; }
 
 ose_corrector* new_corrector() { return new ose_corrector(); }
 void delete_corrector(ose_corrector* c)

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 #include <vector>
 
@@ -44,6 +45,18 @@ struct Net {
     float* loss;           // [0] accumulated loss
 };
 
+// Tensor-core inference (ose_learn_tc.cu): BF16 weights per layer in the
+// kernel's shared-memory layout, biases padded to the layer's N, BF16
+// ping-pong activations [cell][32], and the 8 x 16 x 1 output tiles.
+struct TcNet {
+    int* tiles;
+    int ntiles;
+    uint8_t* w[kLayers];
+    float* b[kLayers];
+    uint16_t* act[2];
+    int* err;              // device error word (a wait that ran out of time)
+};
+
 size_t param_offset(int layer);
 size_t param_count();
 void shell_tiles(const NetGeom& g, std::vector<int>& tiles, long long* ncells, long long* nwrite);
@@ -56,11 +69,23 @@ cudaError_t train_sample(cudaStream_t s, const Net& n, const float2* W, const fl
 // One Adam update with gradients scaled by gscale; clears the gradients.
 cudaError_t adam(cudaStream_t s, const Net& n, float lr, float b1, float b2, float eps, int step, float gscale);
 
+// s = RMS of the state over the shell -> n.scal[1], 1/s -> n.scal[2].
+cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W);
+void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, std::vector<uint8_t>& out);
+void tc_tiles(const NetGeom& g, std::vector<int>& tiles);
+cudaError_t configure_tc();
+// state += s * corrector(state) at the write cells, on the tensor cores.
+cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel);
+
 // Corrector objects (the C ABI's ose_corrector) for the modeler's own use.
 ose_corrector* new_corrector();
 void delete_corrector(ose_corrector* c);
 cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training);
 const Net& net_of(const ose_corrector* c);
+// Tensor-core buffers for inference from FP32 host parameters; err = the
+// device error word the kernels report to.
+cudaError_t create_tc(ose_corrector* c, const float* params_host, int* err);
+const TcNet* tc_of(const ose_corrector* c);
 
 }  // namespace learn
 }  // namespace ose

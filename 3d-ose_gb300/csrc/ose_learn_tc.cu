@@ -1,0 +1,299 @@
+// ose_learn_tc.cu - inference of the boundary corrector on the tcgen05 tensor
+// cores: each 3x3x3 convolution layer is an implicit GEMM with BF16 weights
+// and activations and an FP32 accumulator in TMEM.
+//
+// A CTA computes output tiles of 8 (x) x 16 (y) x 1 (z) = 128 cells, the M
+// rows of the MMA (row m = y * 8 + x).  It stages the input halo of the tile,
+// 10 x 18 x 3 cells with all input channels, once in shared memory in the
+// layout [z 3][y 18][channel chunk][x 10][8 channels x 2 bytes]: for a tap
+// (dx, dy, dz) the 128 x Cin operand is then a plain K-major descriptor into
+// the halo (rows 16 bytes apart, y groups SBO apart, channel chunks LBO apart,
+// start shifted by dx * 16 bytes), so no im2col copy is made.  A tile is
+// 27 taps x Cin / 16 MMAs of 128 x N x 16 (N = 32, or 16 for the 2-channel
+// output layer padded with zero weights), accumulated in TMEM.
+//
+// Layer 0's halo is built from the state and the velocity (the 8 features,
+// padded to 16 channels with zeros); hidden activations are BF16 [cell][32];
+// the output layer adds s * (dP, dQ) to the state at the write cells.  Inputs
+// outside the shell are zero, as in the FP32 kernels (ose_learn.cu).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ose_internal.h"
+#include "ose_learn.h"
+#include "tcgen05.cuh"
+
+namespace ose {
+namespace learn {
+
+namespace {
+
+constexpr int TXW = 8, TYW = 16;              // output tile (x, y), one z plane
+constexpr int HX = TXW + 2, HY = TYW + 2, HZ = 3;
+constexpr int THREADS = 128;                  // one output row (cell) per thread
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+__device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+__device__ __forceinline__ bool in_shell(const NetGeom& g, int x, int y, int z)
+{
+    const int d = min(min(min(x, g.nx - 1 - x), min(y, g.ny - 1 - y)), min(z, g.nz - 1 - z));
+    return d < g.shell;
+}
+
+__device__ __forceinline__ bool is_write(const NetGeom& g, int x, int y, int z)
+{
+    return in_shell(g, x, y, z) && x >= g.sp[0] && x < g.nx - g.sp[1] && y >= g.sp[2] &&
+           y < g.ny - g.sp[3] && z >= g.sp[4] && z < g.nz - g.sp[5];
+}
+
+__device__ __forceinline__ float face_coord(int v, int n, int shell)
+{
+    const int lo = v, hi = n - 1 - v;
+    if (lo < shell && lo <= hi) return -(float)(shell - lo) / (float)shell;
+    if (hi < shell) return (float)(shell - hi) / (float)shell;
+    return 0.f;
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    uint32_t u;
+    memcpy(&u, &h, 4);
+    return u;
+}
+
+template <int CIN, int NPAD>
+struct LayerCfg {
+    static constexpr int chunks = CIN / 8;                       // 16-byte channel chunks
+    static constexpr int halo_bytes = HZ * HY * chunks * HX * 16;
+    static constexpr uint32_t lbo = HX * 16;                     // chunk stride in the halo
+    static constexpr uint32_t sbo = chunks * HX * 16;            // y stride in the halo
+    static constexpr int ngroups = NPAD / 8;
+    static constexpr int w_bytes = 27 * ngroups * chunks * 128;  // B operands, all taps
+    static constexpr uint32_t wsbo = chunks * 128;               // B: n-group stride
+    static constexpr int ksteps = CIN / 16;
+    static constexpr int off_w = halo_bytes;
+    static constexpr int off_bias = off_w + w_bytes;
+    static constexpr int off_bar = off_bias + NPAD * 4;
+    static constexpr int smem = off_bar + 16;
+    static constexpr uint32_t id = tc5::idesc(tc5::kTypeBF16, 128, NPAD);
+};
+
+// MODE 0: layer 0 (features from state + velocity), hidden output (ReLU, BF16)
+// MODE 1: hidden layer, BF16 in, hidden output
+// MODE 2: output layer, BF16 in, state += s * (o0, o1) at the write cells
+template <int CIN, int NPAD, int MODE>
+__global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict__ act_in,
+                                                     const float2* __restrict__ Win, const float* __restrict__ vel,
+                                                     const uint8_t* __restrict__ wts, const float* __restrict__ bias,
+                                                     uint16_t* __restrict__ act_out, float2* __restrict__ state,
+                                                     const float* __restrict__ scal, NetGeom g,
+                                                     const int* __restrict__ tiles, int ntiles, int* err)
+{
+    using C = LayerCfg<CIN, NPAD>;
+    extern __shared__ __align__(1024) uint8_t sm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::off_bar);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::off_bar + 8);
+    float* sb = reinterpret_cast<float*>(sm + C::off_bias);
+    const uint32_t sbase = tc5::smem_u32(sm);
+    const int t = threadIdx.x, warp = t >> 5;
+
+    if (warp == 0) tc5::tmem_alloc(tslot, 32);
+    if (t == 0) tc5::mbar_init(bar, 1);
+    {
+        const int4* s4 = reinterpret_cast<const int4*>(wts);
+        int4* d4 = reinterpret_cast<int4*>(sm + C::off_w);
+        for (int i = t; i < C::w_bytes / 16; i += THREADS) d4[i] = s4[i];
+        for (int i = t; i < NPAD; i += THREADS) sb[i] = bias[i];
+    }
+    const float inv = MODE == 0 ? scal[2] : 0.f;
+    const float sc = MODE == 2 ? scal[1] : 0.f;
+    tc5::fence_before_sync();
+    __syncthreads();
+    tc5::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    int failed = 0;
+    uint32_t phase = 0;
+
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const int tp = tiles[tile];
+        const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
+        // halo: HZ * HY * HX cells x chunks 16-byte units
+        for (int u = t; u < HZ * HY * HX * C::chunks; u += THREADS) {
+            const int ch = u % C::chunks, cell = u / C::chunks;
+            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+            const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (in_shell(g, x, y, z)) {
+                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+                if (MODE == 0) {
+                    if (ch == 0) {
+                        const float2 w = Win[c];
+                        v.x = pack2(w.x * inv, w.y * inv);
+                        v.y = pack2(vel[c] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
+                        v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
+                    }
+                } else {
+                    v = *reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8);
+                }
+            }
+            *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
+        }
+        tc5::fence_async_smem();
+        tc5::fence_before_sync();
+        __syncthreads();
+        int bad = 0;
+        if (t == 0) {
+            tc5::fence_after_sync();
+            uint32_t acc = 0;
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+                const uint32_t a0 = sbase + ((1 + dz) * HY + (1 + dy)) * C::sbo + (1 + dx) * 16;
+                const uint32_t b0 = sbase + C::off_w + tap * C::ngroups * C::chunks * 128;
+#pragma unroll
+                for (int k = 0; k < C::ksteps; ++k) {
+                    const uint64_t da = tc5::smem_desc(a0 + 2 * k * C::lbo, C::lbo, C::sbo);
+                    const uint64_t db = tc5::smem_desc(b0 + 2 * k * 128, 128, C::wsbo);
+                    tc5::mma_f16(tmem, da, db, C::id, acc);
+                    acc = 1;
+                }
+            }
+            tc5::mma_commit(bar);
+            bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
+        }
+        failed = __syncthreads_or(bad);
+        phase ^= 1u;
+        if (failed) break;
+        tc5::fence_after_sync();
+        const int x = x0 + (t & 7), y = y0 + (t >> 3), z = z0;
+        const bool valid = x < g.nx && y < g.ny && in_shell(g, x, y, z);
+        const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+        if (MODE == 2) {
+            float o[16];
+            tc5::tmem_ld16(trow, o);
+            if (valid && is_write(g, x, y, z)) {
+                float2 w = state[c];
+                w.x = fmaf(sc, o[0] + sb[0], w.x);
+                w.y = fmaf(sc, o[1] + sb[1], w.y);
+                state[c] = w;
+            }
+        } else {
+            float o[32];
+            tc5::tmem_ld32(trow, o);
+            if (valid) {
+                uint4* dst = reinterpret_cast<uint4*>(act_out + c * 32);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float* r = o + 8 * q;
+                    const float* b = sb + 8 * q;
+                    dst[q] = make_uint4(pack2(fmaxf(r[0] + b[0], 0.f), fmaxf(r[1] + b[1], 0.f)),
+                                        pack2(fmaxf(r[2] + b[2], 0.f), fmaxf(r[3] + b[3], 0.f)),
+                                        pack2(fmaxf(r[4] + b[4], 0.f), fmaxf(r[5] + b[5], 0.f)),
+                                        pack2(fmaxf(r[6] + b[6], 0.f), fmaxf(r[7] + b[7], 0.f)));
+                }
+            }
+        }
+        tc5::fence_before_sync();
+        __syncthreads();
+    }
+    if (failed && t == 0) {
+        atomicExch(err, 2);
+        tc5::mbar_wait(bar, phase ^ 1u, kWaitLimitNs);
+    }
+    tc5::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc5::fence_after_sync();
+        tc5::tmem_dealloc(tmem, 32);
+    }
+}
+
+uint16_t bf16_bits(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+}  // namespace
+
+// Host: BF16 B operands of one layer in the kernel's shared-memory layout
+// [tap][n group][channel chunk][8 rows][8 channels], zero beyond (cin, cout).
+void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, std::vector<uint8_t>& out)
+{
+    const int chunks = cin_pad / 8, ngroups = npad / 8;
+    out.assign((size_t)27 * ngroups * chunks * 128, 0);
+    for (int tap = 0; tap < 27; ++tap)
+        for (int n = 0; n < npad; ++n)
+            for (int k = 0; k < cin_pad; ++k) {
+                const float v = (n < cout && k < cin) ? w[((size_t)tap * cin + k) * cout + n] : 0.f;
+                const uint16_t b = bf16_bits(v);
+                const size_t o = (((size_t)tap * ngroups + n / 8) * chunks + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+                memcpy(out.data() + o, &b, 2);
+            }
+}
+
+void tc_tiles(const NetGeom& g, std::vector<int>& tiles)
+{
+    tiles.clear();
+    const int tx = (g.nx + TXW - 1) / TXW, ty = (g.ny + TYW - 1) / TYW;
+    for (int z = 0; z < g.nz; ++z)
+        for (int j = 0; j < ty; ++j)
+            for (int i = 0; i < tx; ++i) {
+                bool any = false;
+                for (int y = j * TYW; y < std::min(g.ny, j * TYW + TYW) && !any; ++y)
+                    for (int x = i * TXW; x < std::min(g.nx, i * TXW + TXW) && !any; ++x) {
+                        const int d = std::min(std::min(std::min(x, g.nx - 1 - x), std::min(y, g.ny - 1 - y)),
+                                               std::min(z, g.nz - 1 - z));
+                        any = d < g.shell;
+                    }
+                if (any) tiles.push_back(i | (j << 10) | (z << 20));
+            }
+}
+
+cudaError_t configure_tc()
+{
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_conv_tc<16, 32, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  LayerCfg<16, 32>::smem)) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_conv_tc<32, 32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  LayerCfg<32, 32>::smem)) != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_conv_tc<32, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                LayerCfg<32, 16>::smem);
+}
+
+cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 148;
+    }
+    const unsigned grid = (unsigned)std::max(1, std::min(tc.ntiles, 2 * sms));
+    cudaError_t e = shell_scale(s, n, W);
+    if (e != cudaSuccess) return e;
+    k_conv_tc<16, 32, 0><<<grid, THREADS, LayerCfg<16, 32>::smem, s>>>(
+        nullptr, W, vel, tc.w[0], tc.b[0], tc.act[0], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+    k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
+        tc.act[0], nullptr, nullptr, tc.w[1], tc.b[1], tc.act[1], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+    k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
+        tc.act[1], nullptr, nullptr, tc.w[2], tc.b[2], tc.act[0], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+    k_conv_tc<32, 16, 2><<<grid, THREADS, LayerCfg<32, 16>::smem, s>>>(
+        tc.act[0], nullptr, nullptr, tc.w[3], tc.b[3], nullptr, W, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+    return cudaGetLastError();
+}
+
+}  // namespace learn
+}  // namespace ose

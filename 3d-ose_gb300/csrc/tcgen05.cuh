@@ -1,13 +1,13 @@
 // tcgen05.cuh - the few sm_100-family tensor-core primitives the precision
-// form uses, as inline PTX: TMEM allocation, shared-memory matrix descriptors
-// (K-major, no swizzle), kind::tf32 / kind::f16 MMAs with an FP32 accumulator
-// in TMEM, commit to an mbarrier, a bounded mbarrier wait and TMEM loads.
+// form (ose_tensor.cu) and the boundary corrector (ose_learn_tc.cu) use, as
+// inline PTX: TMEM allocation, shared-memory matrix descriptors (K-major, no
+// swizzle), kind::tf32 / kind::f16 MMAs with an FP32 accumulator in TMEM,
+// commit to an mbarrier, a bounded mbarrier wait and TMEM loads.
 //
 // Operand layout (both A and B, "K-major, no swizzle"): the matrix is cut into
-// core matrices of 8 rows x 16 bytes, each stored as 128 contiguous bytes (row
-// r at r*16).  Core matrices adjacent along K are LBO bytes apart, groups of 8
-// rows are SBO bytes apart.  This file uses LBO = 128 (a row's K cores packed
-// side by side) and SBO = 8 * (bytes of one row).
+// core matrices of 8 rows x 16 bytes whose rows are 16 bytes apart.  Core
+// matrices adjacent along K are LBO bytes apart, groups of 8 rows SBO bytes
+// apart; the start address, LBO and SBO are multiples of 16 bytes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -155,6 +155,23 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
         : "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 16 consecutive FP32 columns of one TMEM lane per thread (shape 32x32b).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // Round to TF32 (nearest, ties away): the FP32 bit pattern with the low 13

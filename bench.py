@@ -284,6 +284,83 @@ def run_precision(args, rank):
     return 0
 
 
+def run_learned(args, rank):
+    """--workload learned: the learned-boundary form.  Padded 256^3 grid =
+    interior 240^3 + 8-cell sponge with the trained corrector on its 16-cell
+    shell (tensor-core inference), against the same interior with a 64-cell
+    sponge (padded 368^3, the plain run the form replaces) and against the thin
+    grid without the corrector.  Reports step rates, the effective rate (cells
+    of the wide grid per second of the learned step) and, over a bounded run,
+    the interior error energy and receiver-gather rel-L2 of both thin runs
+    against the wide run."""
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+    ge.build_library()
+    import ose3d
+    import torch
+    import workloads
+    import learn_boundary as LB
+
+    params = np.load(LB.WEIGHTS)
+    n = 240
+    vel = workloads.smooth_random_salt(n, n, n, seed=505)
+    K = max(1, min(args.steps, 100))
+    acc_steps = 300
+    kw = lambda sp: LB.pair_params(n, 20.0, (120, 120, 8), acc_steps + K + 10, sp)  # noqa: E731
+    res = {}
+    wide_int = []
+    ref_rows = None
+    for mode in ("wide", "plain", "learned"):
+        sp = LB.WIDE if mode == "wide" else LB.THIN
+        m = ose3d.Modeler(ose3d.default_params(**kw(sp)), vel)
+        if mode == "learned":
+            m.set_corrector(params, LB.SHELL)
+        d = m.derived
+        m.reset_shot(0)
+        buf = torch.zeros((n, n, n, 2), dtype=torch.float32, device="cuda")
+        err = ref = 0.0
+        rows = []
+        every = 25
+        for t in range(0, acc_steps, every):
+            rows.append(m.run_record(every))
+            m.state_box(0, (sp, sp, sp, n, n, n), buf.data_ptr(), (n, n, 0, 0, 0))
+            if mode == "wide":
+                wide_int.append(buf.clone())
+            else:
+                w = wide_int[t // every]
+                err += float(((buf - w) ** 2).sum())
+                ref += float((w ** 2).sum())
+        g = np.concatenate(rows)
+        m.run(max(3, args.warmup))
+        ms = m.run_timed(K)
+        prof, _ = m.profile_step(reps=1)
+        cells = d.nxb * d.nyb * d.nzb
+        r = {"grid": [d.nxb, d.nyb, d.nzb], "kernel_path": "generic" if d.path == 0 else "plane",
+             "ms_per_step": ms / K, "gcell_steps_s": cells * K / (ms * 1e-3) / 1e9,
+             "kernels_ms": {p["name"]: p["ms"] * p["launches_per_step"] for p in prof}}
+        if mode == "wide":
+            ref_rows = g
+            wide_cells = cells
+        else:
+            r["interior_error_energy"] = err / max(ref, 1e-300)
+            r["gather_rel_l2"] = float(np.linalg.norm(g - ref_rows) / np.linalg.norm(ref_rows))
+        res[mode] = r
+        m.close()
+    lr = res["learned"]
+    line = {"metric": "effective Gcell-steps/s of the learned-boundary form (cells of the 64-cell-sponge grid it "
+                      "replaces per second)",
+            "value": wide_cells * K / (lr["ms_per_step"] * K * 1e-3) / 1e9, "unit": UNIT, "n_gpus": 1,
+            "steps": K, "warmup": max(3, args.warmup), "ms_per_step": lr["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 solver, bf16 corrector",
+            "data": "synthetic: seeded smooth random 1500-4500 m/s 240^3 interior + salt, 20 Hz Ricker",
+            "config": {"workload": "learned", "interior": [n, n, n], "thin_sponge": LB.THIN,
+                       "wide_sponge": LB.WIDE, "shell": LB.SHELL, "accuracy_steps": acc_steps,
+                       "speedup_vs_wide": res["wide"]["ms_per_step"] / lr["ms_per_step"], "results": res}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,7 +368,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched64", "precision"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched64", "precision", "learned"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -301,6 +378,8 @@ def main():
         return run_batched(args, rank)
     if args.workload == "precision":
         return run_precision(args, rank)
+    if args.workload == "learned":
+        return run_learned(args, rank)
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     dist = Dist(world)

@@ -99,7 +99,7 @@ def loss_and_grads(params_np, P, Q, vel, target_P, target_Q, shell, sponge6):
     w = torch.as_tensor(wr.astype(np.float64))[None]
     loss = (((out - r) ** 2) * w).sum() / wr.sum()
     loss.backward()
-    return float(loss), p.grad.numpy().copy(), out.detach().numpy(), s
+    return float(loss.detach()), p.grad.numpy().copy(), out.detach().numpy(), s
 
 
 def init_params(seed: int = 0, scale: float = 1.0) -> np.ndarray:

@@ -3,7 +3,8 @@ gradient kernels against the FP64 torch-autograd restatement on the CPU
 (oracle/corrector_torch.py), and the corrector inside a modeler's step.
 
 Tolerances: FP32 kernels against FP64 -- output and loss 1e-5 relative,
-gradients 1e-4 relative L2 per layer (sums over ~10^4 products)."""
+gradients 1e-5 relative L2 per layer (sums over ~10^4 products; measured
+about 1.5e-7)."""
 import numpy as np
 import pytest
 
@@ -87,7 +88,7 @@ def test_forward_and_gradients_match_fp64_autograd():
         ew = rel_l2(g[off:off + nw], g64[off:off + nw])
         eb = rel_l2(g[off + nw:off + nw + co], g64[off + nw:off + nw + co])
         print(f"layer {i}: dW {ew:.2e} db {eb:.2e}")
-        assert ew < 1e-4 and eb < 1e-4
+        assert ew < 1e-5 and eb < 1e-5
         off += nw + co
 
 
@@ -139,10 +140,17 @@ def test_zero_corrector_leaves_the_modeler_bitwise_unchanged():
         assert "corrector" in [r["name"] for r in rows]
 
 
-def test_modeler_step_applies_the_corrector():
+@pytest.mark.parametrize("kernels", ["tensor", "fp32"])
+def test_modeler_step_applies_the_corrector(kernels, monkeypatch):
     """One step with a non-zero corrector equals one plain step followed by the
-    training object's apply on the same state."""
+    training object's FP32 apply on the same state: to FP32 rounding with the
+    FP32 kernels, to BF16 rounding of the correction (2e-2 relative) with the
+    tensor-core kernels."""
     torch = pytest.importorskip("torch")
+    if kernels == "fp32":
+        monkeypatch.setenv("OSE3D_CORRECTOR", "fp32")
+    else:
+        monkeypatch.delenv("OSE3D_CORRECTOR", raising=False)
     kw = dict(nx=40, ny=40, nz=40, bu=8, bd=8, bl=8, br=8, bf=8, bb=8, nt=30, fm=25.0, dt=0.002,
               amp=100.0, sxbeg=20, sybeg=20, szbeg=5)
     rng = np.random.default_rng(9)
@@ -167,5 +175,11 @@ def test_modeler_step_applies_the_corrector():
             c.apply(st.data_ptr(), v.data_ptr())
         q = st.cpu().numpy()[..., 1]
         qb = b.wavefield(ose3d.FIELD_Q)
-        assert rel_l2(qb, q) < 1e-6
-        assert not np.array_equal(qb, a.wavefield(ose3d.FIELD_Q))
+        qa = a.wavefield(ose3d.FIELD_Q)
+        assert not np.array_equal(qb, qa)
+        if kernels == "fp32":
+            assert rel_l2(qb, q) < 1e-6
+        else:
+            e = rel_l2(qb.astype(np.float64) - qa, q.astype(np.float64) - qa)
+            print(f"tensor-core correction vs FP32: {e:.2e}")
+            assert e < 2e-2

@@ -1,0 +1,39 @@
+"""The trained boundary corrector (3d-ose_gb300/weights/corrector.npy, made by
+learn_boundary.py train: 200 solver pairs, interior 48^3, 8- vs 64-cell
+sponge) on held-out cases: the thin-sponge run with the corrector against the
+same run without it, both judged by the 64-cell-sponge run.
+
+Measured when the weights were made (4 held-out cases, 300 steps): interior
+error energy 0.24-0.42 without, 0.017-0.045 with the corrector (gain 9-20x);
+gather rel-L2 0.63-1.48 without, 0.21-0.50 with.  The test asks for a gain of
+at least 4x on two other cases over 200 steps."""
+import os
+
+import numpy as np
+import pytest
+
+import ose3d
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as ge
+    ge.build_library()
+    ose3d.load_library()
+
+
+def test_trained_corrector_reduces_boundary_error():
+    pytest.importorskip("torch")
+    import learn_boundary as LB
+    assert os.path.exists(LB.WEIGHTS)
+    params = np.load(LB.WEIGHTS)
+    assert params.size == ose3d.corrector_param_count()
+    res = LB.evaluate(params, seed=4242, cases=2, n=48, steps=200)
+    for r in res:
+        print(f"fm {r['fm']:.1f} Hz: error energy {r['plain']['interior_error_energy']:.3e} -> "
+              f"{r['learned']['interior_error_energy']:.3e} (gain {r['gain']:.1f}x), gather "
+              f"{r['plain']['gather_rel_l2']:.3f} -> {r['learned']['gather_rel_l2']:.3f}")
+        assert r["gain"] > 4.0
+        assert r["learned"]["gather_rel_l2"] < r["plain"]["gather_rel_l2"]
