@@ -8,7 +8,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <complex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ose_internal.h"
@@ -173,13 +175,13 @@ cudaError_t enqueue_corrector(ose_handle* h, ose::KernelTiming* tm)
 // Plane path step: 2 HBM passes per operator application (ose_plane.cu).
 // Timing classes: 0 plane_fwd, 1 zpass, 2 plane_inv_first, 3 plane_inv_mid,
 // 4 plane_inv_last, 5 inject.
-cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
+cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm, bool source)
 {
     cudaStream_t s = h->stream;
     const double N = (double)h->g.ncell;
-    cudaError_t e = timed(tm, s, 5, 16.0, [&] {
+    cudaError_t e = source ? timed(tm, s, 5, 16.0, [&] {
         return ose::launch_inject(s, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
-    });
+    }) : cudaSuccess;
     if (e != cudaSuccess) return e;
     const int M = h->d.M;
     ose::EpiArgs ea{};
@@ -230,13 +232,13 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm)
 }
 
 // Enqueue one whole time step on h->stream (no synchronisation).
-cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm)
+// source = false leaves out the source injection (reverse-time propagation).
+cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = true)
 {
-    if (h->d.path == OSE_PATH_PLANE) return enqueue_step_plane(h, tm);
-    cudaError_t e;
-    e = timed(tm, h->stream, 5, 16.0, [&] {
+    if (h->d.path == OSE_PATH_PLANE) return enqueue_step_plane(h, tm, source);
+    cudaError_t e = source ? timed(tm, h->stream, 5, 16.0, [&] {
         return ose::launch_inject(h->stream, h->W, h->src, h->ricker, h->hil, h->ctr, h->p.nt);
-    });
+    }) : cudaSuccess;
     if (e != cudaSuccess) return e;
     const int M = h->d.M;
     ose::EpiArgs ea{};
@@ -764,6 +766,166 @@ ose_status ose_state_box(ose_handle* h, int dir, const int* box, void* buf_dev, 
     CK(h, cudaGetLastError());
     CK(h, cudaStreamSynchronize(h->stream));
     return OSE_OK;
+}
+
+namespace {
+
+// P of the state -> snap (the source wavefield of reverse-time migration).
+__global__ void k_take_p(const float2* __restrict__ W, float* __restrict__ snap, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        snap[i] = W[i].x;
+}
+
+// Reverse-time injection of one gather row at the receivers (the cells the
+// LAST epilogue records): P += p[ig], Q += q[ig].
+__global__ void k_inject_row(float2* __restrict__ W, const float* __restrict__ p, const float* __restrict__ q, int gz,
+                             int bl, int bf, int nx, int ny, int nxb, int nyb)
+{
+    const int ig = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ig >= nx * ny) return;
+    const int iy = ig / nx, ix = ig - iy * nx;
+    float2& w = W[((size_t)gz * nyb + (bf + iy)) * nxb + (bl + ix)];
+    w.x += p[ig];
+    w.y += q[ig];
+}
+
+// Zero-lag cross-correlation imaging condition: image += P_source * P_receiver.
+__global__ void k_image(float* __restrict__ img, const float* __restrict__ snap, const float2* __restrict__ W,
+                        long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        img[i] = fmaf(snap[i], W[i].x, img[i]);
+}
+
+// In-place radix-2 FFT of length n (a power of two), sign -1 forward.
+void fft_pow2(std::vector<std::complex<double>>& a, int sign)
+{
+    const size_t n = a.size();
+    for (size_t i = 1, j = 0; i < n; ++i) {
+        size_t bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(a[i], a[j]);
+    }
+    const double pi = 3.14159265358979323846;
+    for (size_t len = 2; len <= n; len <<= 1) {
+        const std::complex<double> wl(cos(2 * pi / (double)len), sign * sin(2 * pi / (double)len));
+        for (size_t i = 0; i < n; i += len) {
+            std::complex<double> w(1.0, 0.0);
+            for (size_t k = 0; k < len / 2; ++k) {
+                const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w;
+                a[i + k] = u + v;
+                a[i + k + len / 2] = u - v;
+                w *= wl;
+            }
+        }
+    }
+}
+
+// Hilbert transform of every receiver trace of rows [nsteps][ng] (zero padded
+// to a power of two >= 2 nsteps, so the transform does not wrap around):
+// h = IFFT(-i sgn(f) FFT(d)).  Spread over the host threads.
+void hilbert_rows(const float* rows, int nsteps, int ng, std::vector<float>& out)
+{
+    out.assign((size_t)nsteps * ng, 0.f);
+    size_t L = 1;
+    while (L < 2 * (size_t)nsteps) L <<= 1;
+    const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+    auto work = [&](int t0) {
+        std::vector<std::complex<double>> a(L);
+        for (int ig = t0; ig < ng; ig += nth) {
+            for (size_t i = 0; i < L; ++i) a[i] = i < (size_t)nsteps ? rows[i * ng + ig] : 0.0;
+            fft_pow2(a, -1);
+            for (size_t k = 0; k < L; ++k) {
+                if (k == 0 || k == L / 2) a[k] = 0.0;
+                else if (k < L / 2) a[k] *= std::complex<double>(0.0, -1.0);
+                else a[k] *= std::complex<double>(0.0, 1.0);
+            }
+            fft_pow2(a, +1);
+            for (int i = 0; i < nsteps; ++i) out[(size_t)i * ng + ig] = (float)(a[i].real() / (double)L);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image)
+{
+    if (!h || !rows || !image || nsteps < 1 || every < 1) return OSE_ERR_INVALID;
+    if (nsteps > h->p.nt) return fail(h, OSE_ERR_INVALID, "nsteps beyond nt");
+    const size_t N = (size_t)h->g.ncell;
+    const int ng = h->d.ng;
+    const int nsnap = nsteps / every + 1;
+    size_t free_b = 0, total_b = 0;
+    CK(h, cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = sizeof(float) * (N * (size_t)(nsnap + 1) + 2 * (size_t)nsteps * ng);
+    if (need + ((size_t)1 << 30) > free_b)
+        return fail(h, OSE_ERR_NOMEM, "reverse-time migration needs " + std::to_string(need >> 20) +
+                                          " MiB of device memory for its snapshots");
+    std::vector<float> hil;
+    hilbert_rows(rows, nsteps, ng, hil);
+    // the observed rows are the Q part (the receivers record Q); their analytic
+    // pair is P = -H[d], Q = d, and time reversal conjugates it: inject
+    // P += -h(t), Q += -d(t) while stepping backwards
+    std::vector<float> pin((size_t)nsteps * ng), qin((size_t)nsteps * ng);
+    for (size_t i = 0; i < pin.size(); ++i) {
+        pin[i] = -hil[i];
+        qin[i] = -rows[i];
+    }
+    float *snaps = nullptr, *img = nullptr, *dp = nullptr, *dq = nullptr;
+    auto release = [&] {
+        for (float* b : {snaps, img, dp, dq})
+            if (b) cudaFree(b);
+    };
+#define CKR(call)                                                    \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) { release(); return cuda_fail(h, e_, #call); } \
+    } while (0)
+    CKR(cudaMalloc((void**)&snaps, sizeof(float) * N * nsnap));
+    CKR(cudaMalloc((void**)&img, sizeof(float) * N));
+    CKR(cudaMalloc((void**)&dp, sizeof(float) * pin.size()));
+    CKR(cudaMalloc((void**)&dq, sizeof(float) * qin.size()));
+    CKR(cudaMemcpyAsync(dp, pin.data(), sizeof(float) * pin.size(), cudaMemcpyHostToDevice, h->stream));
+    CKR(cudaMemcpyAsync(dq, qin.data(), sizeof(float) * qin.size(), cudaMemcpyHostToDevice, h->stream));
+    CKR(cudaMemsetAsync(img, 0, sizeof(float) * N, h->stream));
+    CKR(cudaMemsetAsync(snaps, 0, sizeof(float) * N, h->stream));   // time 0: at rest
+    const unsigned blocks = (unsigned)std::min<size_t>(8192, (N + 255) / 256);
+    // forward: the source wavefield, P kept every `every` steps
+    ose_status st = ose_reset_shot(h, h->shot >= 0 ? h->shot : 0);
+    if (st != OSE_OK) { release(); return st; }
+    st = build_graph(h);
+    if (st != OSE_OK) { release(); return st; }
+    for (int it = 0; it < nsteps; ++it) {
+        CKR(cudaGraphLaunch(h->graph, h->stream));
+        if ((it + 1) % every == 0)
+            k_take_p<<<blocks, 256, 0, h->stream>>>(h->W, snaps + N * (size_t)((it + 1) / every), (long long)N);
+    }
+    // backward: receiver wavefield from the time-reversed rows, no source, no recording
+    CKR(cudaMemsetAsync(h->W, 0, sizeof(float2) * N, h->stream));
+    const int no_record[2] = {0, -1};
+    CKR(cudaMemcpyAsync(h->ctr, no_record, sizeof(no_record), cudaMemcpyHostToDevice, h->stream));
+    const int gz = h->p.bu + h->p.gzbeg;
+    for (int it = nsteps - 1; it >= 0; --it) {
+        k_inject_row<<<(ng + 255) / 256, 256, 0, h->stream>>>(h->W, dp + (size_t)it * ng, dq + (size_t)it * ng, gz,
+                                                                h->p.bl, h->p.bf, h->p.nx, h->p.ny, h->d.nxb, h->d.nyb);
+        CKR(enqueue_step(h, nullptr, false));
+        if (it % every == 0)
+            k_image<<<blocks, 256, 0, h->stream>>>(img, snaps + N * (size_t)(it / every), h->W, (long long)N);
+    }
+    CKR(cudaGetLastError());
+    CKR(cudaMemcpyAsync(image, img, sizeof(float) * N, cudaMemcpyDeviceToHost, h->stream));
+    CKR(cudaStreamSynchronize(h->stream));
+#undef CKR
+    release();
+    // the state now holds the receiver wavefield: a new shot must be started
+    h->shot_ready = false;
+    h->it = 0;
+    return tensor_status(h);
 }
 
 ose_status ose_get_it(const ose_handle* h, int* it)

@@ -125,26 +125,60 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const int tp = tiles[tile];
         const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
-        // halo: HZ * HY * HX cells x chunks 16-byte units
-        for (int u = t; u < HZ * HY * HX * C::chunks; u += THREADS) {
-            const int ch = u % C::chunks, cell = u / C::chunks;
-            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-            const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (in_shell(g, x, y, z)) {
+        // halo: HZ * HY * HX cells x chunks 16-byte units; every load of the
+        // thread is issued before the first store so they overlap
+        constexpr int UNITS = HZ * HY * HX * C::chunks;
+        constexpr int PER = (UNITS + THREADS - 1) / THREADS;
+        if (MODE == 0) {
+            float2 wv[PER];
+            float vv[PER];
+            bool ok[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                ok[k] = u < UNITS && ch == 0 && in_shell(g, x, y, z);
                 const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-                if (MODE == 0) {
-                    if (ch == 0) {
-                        const float2 w = Win[c];
-                        v.x = pack2(w.x * inv, w.y * inv);
-                        v.y = pack2(vel[c] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
-                        v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
-                    }
-                } else {
-                    v = *reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8);
-                }
+                wv[k] = ok[k] ? __ldg(Win + c) : make_float2(0.f, 0.f);
+                vv[k] = ok[k] ? __ldg(vel + c) : 0.f;
             }
-            *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                if (u >= UNITS) break;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (ok[k]) {
+                    const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                    v.x = pack2(wv[k].x * inv, wv[k].y * inv);
+                    v.y = pack2(vv[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
+                    v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
+                }
+                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
+            }
+        } else {
+            uint4 v[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                const bool ok = u < UNITS && in_shell(g, x, y, z);
+                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+                v[k] = ok ? __ldg(reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8)) : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                if (u >= UNITS) break;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v[k];
+            }
         }
         tc5::fence_async_smem();
         tc5::fence_before_sync();

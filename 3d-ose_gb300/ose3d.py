@@ -43,7 +43,8 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_state_box", "ose_corrector_param_count", "ose_corrector_create", "ose_corrector_destroy",
            "ose_corrector_last_error", "ose_corrector_info", "ose_corrector_set_params",
            "ose_corrector_get_params", "ose_corrector_get_grads", "ose_corrector_forward",
-           "ose_corrector_apply", "ose_corrector_train_sample", "ose_corrector_adam", "ose_corrector_loss"]
+           "ose_corrector_apply", "ose_corrector_train_sample", "ose_corrector_adam", "ose_corrector_loss",
+           "ose_rtm"]
 CORRECTOR_SHELL = 16   # OSE_CORRECTOR_SHELL
 
 # void (*)(int it, const float* P, const float* Q, void* user)
@@ -122,6 +123,7 @@ def load_library(path: str = LIB_PATH):
         "ose_select_path": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_precision": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_corrector": ([H, f32, ctypes.c_int], ctypes.c_int),
+        "ose_rtm": ([H, f32, ctypes.c_int, ctypes.c_int, f32], ctypes.c_int),
         "ose_state_box": ([H, ctypes.c_int, P(ctypes.c_int), ctypes.c_void_p, P(ctypes.c_int)], ctypes.c_int),
         "ose_corrector_param_count": ([], ctypes.c_size_t),
         "ose_corrector_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), P(H)],
@@ -510,6 +512,15 @@ class Modeler:
             return
         p = np.ascontiguousarray(params, np.float32)
         self._check(self._lib.ose_set_corrector(self._h, _f32(p), shell))
+
+    def rtm(self, rows: np.ndarray, every: int = 4) -> np.ndarray:
+        """Reverse-time migration of the current shot's observed receiver rows
+        ([it][ig], as run_record returns them) with this modeler's velocity;
+        returns the padded [z][y][x] image."""
+        r = np.ascontiguousarray(rows, np.float32)
+        img = np.zeros(self.shape, np.float32)
+        self._check(self._lib.ose_rtm(self._h, _f32(r), r.shape[0], every, _f32(img)))
+        return img
 
     def state_box(self, direction: int, box, buf_ptr: int, buf):
         """Copy a box of the state to (direction 0) or from (1) a device

@@ -233,6 +233,18 @@ ose_status ose_corrector_adam(ose_corrector* c, float lr, int batch, float* mean
 /* Accumulated loss; reset != 0 also clears it and the gradients. */
 ose_status ose_corrector_loss(ose_corrector* c, float* loss, int reset);
 
+/* Reverse-time migration of the current shot (ose_3d.cu:127 names an "rtm
+ * result"; the reference has no migration code): forward-propagate the source
+ * for nsteps steps keeping P on the device every `every` steps, then
+ * propagate the observed receiver rows (host, nsteps x ng, [it][ig] as
+ * ose_run_record returns them; the receivers record Q) backwards in time,
+ * injected at the receivers as their analytic pair, and accumulate the
+ * zero-lag cross-correlation image += P_source * P_receiver at the kept steps.
+ * image: padded [z][y][x] floats.  Device memory: nsteps/every + 1 padded
+ * fields.  Uses the handle's model as the migration velocity; afterwards the
+ * state is the receiver wavefield and a new ose_reset_shot is needed. */
+ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image);
+
 /* Steps taken in the current shot. */
 ose_status ose_get_it(const ose_handle* h, int* it);
 
