@@ -790,12 +790,16 @@ __global__ void k_inject_row(float2* __restrict__ W, const float* __restrict__ p
     w.y += q[ig];
 }
 
-// Zero-lag cross-correlation imaging condition: image += P_source * P_receiver.
-__global__ void k_image(float* __restrict__ img, const float* __restrict__ snap, const float2* __restrict__ W,
-                        long long n)
+// Zero-lag cross-correlation imaging condition: image += P_source * P_receiver,
+// and the source illumination ill += P_source^2.
+__global__ void k_image(float* __restrict__ img, float* __restrict__ ill, const float* __restrict__ snap,
+                        const float2* __restrict__ W, long long n)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        img[i] = fmaf(snap[i], W[i].x, img[i]);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float s = snap[i];
+        img[i] = fmaf(s, W[i].x, img[i]);
+        ill[i] = fmaf(s, s, ill[i]);
+    }
 }
 
 // In-place radix-2 FFT of length n (a power of two), sign -1 forward.
@@ -853,7 +857,7 @@ void hilbert_rows(const float* rows, int nsteps, int ng, std::vector<float>& out
 
 }  // namespace
 
-ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image)
+ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image, float* illum)
 {
     if (!h || !rows || !image || nsteps < 1 || every < 1) return OSE_ERR_INVALID;
     if (nsteps > h->p.nt) return fail(h, OSE_ERR_INVALID, "nsteps beyond nt");
@@ -862,23 +866,26 @@ ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, floa
     const int nsnap = nsteps / every + 1;
     size_t free_b = 0, total_b = 0;
     CK(h, cudaMemGetInfo(&free_b, &total_b));
-    const size_t need = sizeof(float) * (N * (size_t)(nsnap + 1) + 2 * (size_t)nsteps * ng);
+    const size_t need = sizeof(float) * (N * (size_t)(nsnap + 2) + 2 * (size_t)nsteps * ng);
     if (need + ((size_t)1 << 30) > free_b)
         return fail(h, OSE_ERR_NOMEM, "reverse-time migration needs " + std::to_string(need >> 20) +
                                           " MiB of device memory for its snapshots");
     std::vector<float> hil;
     hilbert_rows(rows, nsteps, ng, hil);
-    // the observed rows are the Q part (the receivers record Q); their analytic
-    // pair is P = -H[d], Q = d, and time reversal conjugates it: inject
-    // P += -h(t), Q += -d(t) while stepping backwards
+    // The step is W(t + dt) = exp(-i v|k| dt) W(t), so a free wave has
+    // P = H[Q] along time (H: the Hilbert transform, -i on positive
+    // frequencies).  The receivers record Q = d, hence P = h = H[d].  Run
+    // backwards, W_rev(tau) = conj(W(T - tau)) obeys the same step with the
+    // source -conj(P + iQ): inject P += -h(t), Q += +d(t) at t = T - tau.
+    // (Checked by refocusing a recorded point source at its position.)
     std::vector<float> pin((size_t)nsteps * ng), qin((size_t)nsteps * ng);
     for (size_t i = 0; i < pin.size(); ++i) {
         pin[i] = -hil[i];
-        qin[i] = -rows[i];
+        qin[i] = rows[i];
     }
-    float *snaps = nullptr, *img = nullptr, *dp = nullptr, *dq = nullptr;
+    float *snaps = nullptr, *img = nullptr, *ill = nullptr, *dp = nullptr, *dq = nullptr;
     auto release = [&] {
-        for (float* b : {snaps, img, dp, dq})
+        for (float* b : {snaps, img, ill, dp, dq})
             if (b) cudaFree(b);
     };
 #define CKR(call)                                                    \
@@ -888,6 +895,8 @@ ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, floa
     } while (0)
     CKR(cudaMalloc((void**)&snaps, sizeof(float) * N * nsnap));
     CKR(cudaMalloc((void**)&img, sizeof(float) * N));
+    CKR(cudaMalloc((void**)&ill, sizeof(float) * N));
+    CKR(cudaMemsetAsync(ill, 0, sizeof(float) * N, h->stream));
     CKR(cudaMalloc((void**)&dp, sizeof(float) * pin.size()));
     CKR(cudaMalloc((void**)&dq, sizeof(float) * qin.size()));
     CKR(cudaMemcpyAsync(dp, pin.data(), sizeof(float) * pin.size(), cudaMemcpyHostToDevice, h->stream));
@@ -915,10 +924,11 @@ ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, floa
                                                                 h->p.bl, h->p.bf, h->p.nx, h->p.ny, h->d.nxb, h->d.nyb);
         CKR(enqueue_step(h, nullptr, false));
         if (it % every == 0)
-            k_image<<<blocks, 256, 0, h->stream>>>(img, snaps + N * (size_t)(it / every), h->W, (long long)N);
+            k_image<<<blocks, 256, 0, h->stream>>>(img, ill, snaps + N * (size_t)(it / every), h->W, (long long)N);
     }
     CKR(cudaGetLastError());
     CKR(cudaMemcpyAsync(image, img, sizeof(float) * N, cudaMemcpyDeviceToHost, h->stream));
+    if (illum) CKR(cudaMemcpyAsync(illum, ill, sizeof(float) * N, cudaMemcpyDeviceToHost, h->stream));
     CKR(cudaStreamSynchronize(h->stream));
 #undef CKR
     release();

@@ -123,7 +123,7 @@ def load_library(path: str = LIB_PATH):
         "ose_select_path": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_precision": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_corrector": ([H, f32, ctypes.c_int], ctypes.c_int),
-        "ose_rtm": ([H, f32, ctypes.c_int, ctypes.c_int, f32], ctypes.c_int),
+        "ose_rtm": ([H, f32, ctypes.c_int, ctypes.c_int, f32, f32], ctypes.c_int),
         "ose_state_box": ([H, ctypes.c_int, P(ctypes.c_int), ctypes.c_void_p, P(ctypes.c_int)], ctypes.c_int),
         "ose_corrector_param_count": ([], ctypes.c_size_t),
         "ose_corrector_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), P(H)],
@@ -513,14 +513,15 @@ class Modeler:
         p = np.ascontiguousarray(params, np.float32)
         self._check(self._lib.ose_set_corrector(self._h, _f32(p), shell))
 
-    def rtm(self, rows: np.ndarray, every: int = 4) -> np.ndarray:
+    def rtm(self, rows: np.ndarray, every: int = 4):
         """Reverse-time migration of the current shot's observed receiver rows
         ([it][ig], as run_record returns them) with this modeler's velocity;
-        returns the padded [z][y][x] image."""
+        returns the padded [z][y][x] image and source illumination."""
         r = np.ascontiguousarray(rows, np.float32)
         img = np.zeros(self.shape, np.float32)
-        self._check(self._lib.ose_rtm(self._h, _f32(r), r.shape[0], every, _f32(img)))
-        return img
+        ill = np.zeros(self.shape, np.float32)
+        self._check(self._lib.ose_rtm(self._h, _f32(r), r.shape[0], every, _f32(img), _f32(ill)))
+        return img, ill
 
     def state_box(self, direction: int, box, buf_ptr: int, buf):
         """Copy a box of the state to (direction 0) or from (1) a device

@@ -240,10 +240,12 @@ ose_status ose_corrector_loss(ose_corrector* c, float* loss, int reset);
  * ose_run_record returns them; the receivers record Q) backwards in time,
  * injected at the receivers as their analytic pair, and accumulate the
  * zero-lag cross-correlation image += P_source * P_receiver at the kept steps.
- * image: padded [z][y][x] floats.  Device memory: nsteps/every + 1 padded
- * fields.  Uses the handle's model as the migration velocity; afterwards the
- * state is the receiver wavefield and a new ose_reset_shot is needed. */
-ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image);
+ * image: padded [z][y][x] floats; illum (may be NULL): the source
+ * illumination sum P_source^2 at the same steps, the usual normaliser of the
+ * image.  Device memory: nsteps/every + 3 padded fields.  Uses the handle's
+ * model as the migration velocity; afterwards the state is the receiver
+ * wavefield at time 0 and a new ose_reset_shot is needed to step again. */
+ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, float* image, float* illum);
 
 /* Steps taken in the current shot. */
 ose_status ose_get_it(const ose_handle* h, int* it);
