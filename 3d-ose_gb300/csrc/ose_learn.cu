@@ -6,16 +6,19 @@
 //
 // Network (fixed architecture, 64,034 parameters):
 //   input  8 channels per cell: P/s, Q/s, v/4500, ex, ey, ez, 0, 0
-//          s = RMS of (P, Q) over the shell; e. = signed closeness to the
-//          nearest face of that axis inside the shell, -1 .. 1, 0 beyond it
+//          s = s(x), the local RMS of (P, Q): sqrt(m/2 + f^2), m the mean of
+//          P^2 + Q^2 over the 17^3 box around the cell (shell cells only), f
+//          = 1e-3 x the RMS over the whole shell (a floor for empty regions);
+//          e. = signed closeness to the nearest face of that axis inside the
+//          shell, -1 .. 1, 0 beyond it
 //   conv 3x3x3  8 -> 32, ReLU
 //   conv 3x3x3 32 -> 32, ReLU
 //   conv 3x3x3 32 -> 32, ReLU
-//   conv 3x3x3 32 ->  2      output (dP, dQ) / s
+//   conv 3x3x3 32 ->  2      output (dP, dQ) / s(x)
 // The network lives on the SHELL: cells within `shell` cells of a face of the
 // padded grid (periodic, like the FFT grid, so opposite faces are neighbours).
-// Every layer reads zeros outside the shell.  The correction s * (dP, dQ) is
-// added to the state at the WRITE cells: shell cells outside the sponge.
+// Every layer reads zeros outside the shell.  The correction s(x) (dP, dQ)
+// is added to the state at the WRITE cells: shell cells outside the sponge.
 //
 // Layout: activations are dense channels-last float arrays [cell][C] over the
 // padded grid, cell = (z * nyb + y) * nxb + x; only shell cells are computed
@@ -99,10 +102,62 @@ __global__ void k_shell_scale(float* scal, float inv_count2)
     scal[2] = s > 0.f ? 1.f / s : 0.f;
 }
 
-__global__ void k_features(const float2* __restrict__ W, const float* __restrict__ vel, const float* __restrict__ scal,
+// Local scale s(x): three periodic box sums of P^2 + Q^2 (shell cells) with
+// half-width kBoxR, x then y then z over the whole padded grid.
+constexpr int kBoxR = 8;
+
+__global__ void k_box_x(const float2* __restrict__ W, float* __restrict__ out, NetGeom g)
+{
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx);
+        const long long row = i - x;
+        const int y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+        float acc = 0.f;
+        for (int d = -kBoxR; d <= kBoxR; ++d) {
+            const int xn = wrapi(x + d, g.nx);
+            if (in_shell(g, xn, y, z)) {
+                const float2 w = W[row + xn];
+                acc = fmaf(w.x, w.x, fmaf(w.y, w.y, acc));
+            }
+        }
+        out[i] = acc;
+    }
+}
+
+__global__ void k_box_y(const float* __restrict__ in, float* __restrict__ out, NetGeom g)
+{
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny);
+        const long long base = i - (long long)y * g.nx;
+        float acc = 0.f;
+        for (int d = -kBoxR; d <= kBoxR; ++d) acc += in[base + (long long)wrapi(y + d, g.ny) * g.nx];
+        out[i] = acc;
+        (void)x;
+    }
+}
+
+// z sum, then s = sqrt(m / 2 + f^2) with m the box mean and f = 1e-3 s_shell.
+__global__ void k_box_z(const float* __restrict__ in, float* __restrict__ sloc, const float* __restrict__ scal,
+                        NetGeom g)
+{
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    const long long plane = (long long)g.nx * g.ny;
+    const float f = 1e-3f * scal[1];
+    const float inv_vol = 1.f / (float)((2 * kBoxR + 1) * (2 * kBoxR + 1) * (2 * kBoxR + 1));
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(i / plane);
+        const long long base = i - (long long)z * plane;
+        float acc = 0.f;
+        for (int d = -kBoxR; d <= kBoxR; ++d) acc += in[base + (long long)wrapi(z + d, g.nz) * plane];
+        sloc[i] = sqrtf(0.5f * acc * inv_vol + f * f);
+    }
+}
+
+__global__ void k_features(const float2* __restrict__ W, const float* __restrict__ vel, const float* __restrict__ sloc,
                            float* __restrict__ F, NetGeom g, const int* __restrict__ tiles, int ntiles)
 {
-    const float inv = scal[2];
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         int x0, y0, z0;
         tile_origin(tiles[tile], x0, y0, z0);
@@ -111,6 +166,7 @@ __global__ void k_features(const float2* __restrict__ W, const float* __restrict
             if (x >= g.nx || y >= g.ny || z >= g.nz || !in_shell(g, x, y, z)) continue;
             const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
             const float2 w = W[c];
+            const float inv = 1.f / sloc[c];
             float4* f = reinterpret_cast<float4*>(F + c * 8);
             f[0] = make_float4(w.x * inv, w.y * inv, vel[c] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
             f[1] = make_float4(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell), 0.f, 0.f);
@@ -123,7 +179,7 @@ __global__ void k_features(const float2* __restrict__ W, const float* __restrict
 //   MODE_RELU   out = max(0, acc)
 //   MODE_LINEAR out = acc
 //   MODE_MASK   out = acc * (mask[c][co] > 0)   (data gradient through a ReLU)
-//   MODE_APPLY  state[c] += s * (acc0, acc1) at the write cells (COUT = 2)
+//   MODE_APPLY  state[c] += s(c) * (acc0, acc1) at the write cells (COUT = 2)
 enum { MODE_RELU = 0, MODE_LINEAR = 1, MODE_MASK = 2, MODE_APPLY = 3 };
 
 template <int CIN, int COUT, int MODE>
@@ -193,14 +249,15 @@ __global__ void __launch_bounds__(kThreads) k_conv(const float* __restrict__ in,
         }
         const size_t ca = ((size_t)za * g.ny + y) * g.nx + x, cb = ((size_t)zb * g.ny + y) * g.nx + x;
         if (MODE == MODE_APPLY) {
-            const float s = scal[1];
             if (va && is_write(g, x, y, za)) {
+                const float s = scal[ca];
                 float2 v = state[ca];
                 v.x = fmaf(s, a[0], v.x);
                 v.y = fmaf(s, a[1], v.y);
                 state[ca] = v;
             }
             if (vb && is_write(g, x, y, zb)) {
+                const float s = scal[cb];
                 float2 v = state[cb];
                 v.x = fmaf(s, b[0], v.x);
                 v.y = fmaf(s, b[1], v.y);
@@ -303,13 +360,12 @@ __global__ void k_bgrad(const float* __restrict__ gout, float* __restrict__ gb, 
     for (int i = threadIdx.x; i < COUT; i += blockDim.x) atomicAdd(gb + i, red[i]);
 }
 
-// Loss of one sample: r = (target - state) / s at the write cells, the
+// Loss of one sample: r = (target - state) / s(x) at the write cells, the
 // network output o (normalised units); g = 2 (o - r) / nw, loss += |o - r|^2 / nw.
 __global__ void k_loss(const float* __restrict__ o, const float2* __restrict__ state, const float2* __restrict__ tgt,
-                       const float* __restrict__ scal, float* __restrict__ gout, float* loss, float inv_nw, NetGeom g,
+                       const float* __restrict__ sloc, float* __restrict__ gout, float* loss, float inv_nw, NetGeom g,
                        const int* __restrict__ tiles, int ntiles)
 {
-    const float inv = scal[2];
     float l = 0.f;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         int x0, y0, z0;
@@ -320,6 +376,7 @@ __global__ void k_loss(const float* __restrict__ o, const float2* __restrict__ s
             const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
             float gx = 0.f, gy = 0.f;
             if (is_write(g, x, y, z)) {
+                const float inv = 1.f / sloc[c];
                 const float2 u = state[c], v = tgt[c];
                 const float ex = o[2 * c] - (v.x - u.x) * inv, ey = o[2 * c + 1] - (v.y - u.y) * inv;
                 gx = 2.f * ex * inv_nw;
@@ -442,6 +499,11 @@ cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
     const unsigned gr = grid_for(n.ntiles, 2);
     k_shell_sumsq<<<gr, 256, 0, s>>>(W, n.g, n.tiles, n.ntiles, n.scal);
     k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
+    const long long cells = (long long)n.g.nx * n.g.ny * n.g.nz;
+    const unsigned gb = (unsigned)std::min<long long>(4096, (cells + 255) / 256);
+    k_box_x<<<gb, 256, 0, s>>>(W, n.sloc, n.g);
+    k_box_y<<<gb, 256, 0, s>>>(n.sloc, n.stmp, n.g);
+    k_box_z<<<gb, 256, 0, s>>>(n.stmp, n.sloc, n.scal, n.g);
     return cudaGetLastError();
 }
 
@@ -452,7 +514,7 @@ cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* 
     const unsigned gr = grid_for(n.ntiles, 2);
     cudaError_t e0 = shell_scale(s, n, W);
     if (e0 != cudaSuccess) return e0;
-    k_features<<<gr, 256, 0, s>>>(W, vel, n.scal, n.F, g, n.tiles, n.ntiles);
+    k_features<<<gr, 256, 0, s>>>(W, vel, n.sloc, n.F, g, n.tiles, n.ntiles);
     const float* w0 = p + param_offset(0);
     const float* w1 = p + param_offset(1);
     const float* w2 = p + param_offset(2);
@@ -465,7 +527,7 @@ cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* 
                                                                      nullptr, n.scal, g, n.tiles, n.ntiles);
     if (apply)
         k_conv<32, 2, MODE_APPLY><<<gr, kThreads, 27 * 32 * 2 * 4, s>>>(n.A[2], w3, w3 + 27 * 32 * 2, nullptr,
-                                                                        nullptr, state_out, n.scal, g, n.tiles,
+                                                                        nullptr, state_out, n.sloc, g, n.tiles,
                                                                         n.ntiles);
     else
         k_conv<32, 2, MODE_LINEAR><<<gr, kThreads, 27 * 32 * 2 * 4, s>>>(n.A[2], w3, w3 + 27 * 32 * 2, n.O, nullptr,
@@ -480,7 +542,7 @@ cudaError_t train_sample(cudaStream_t s, const Net& n, const float2* W, const fl
     const NetGeom& g = n.g;
     const unsigned gr = grid_for(n.ntiles, 2);
     const unsigned gw = grid_for(n.ntiles, 1);
-    k_loss<<<gr, 256, 0, s>>>(n.O, W, tgt, n.scal, n.G4, n.loss, (float)(1.0 / (double)std::max(1LL, n.nwrite)), g,
+    k_loss<<<gr, 256, 0, s>>>(n.O, W, tgt, n.sloc, n.G4, n.loss, (float)(1.0 / (double)std::max(1LL, n.nwrite)), g,
                               n.tiles, n.ntiles);
     float* gp = n.grads;
     // data-gradient weights of layers 1..3 (layer 0's input needs none)
@@ -583,6 +645,8 @@ cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training)
     A_(n.params, np);
     A_(n.scal, 4);
     A_(n.loss, 1);
+    A_(n.sloc, cells);
+    A_(n.stmp, cells);
     A_(n.F, cells * 8);
     for (int l = 0; l < 3; ++l) A_(n.A[l], cells * 32);
     if (training) {

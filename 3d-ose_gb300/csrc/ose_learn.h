@@ -41,7 +41,9 @@ struct Net {
     float* O;              // [cell][2] output
     float* G4;             // [cell][2] output gradient
     float* GA[3];          // [cell][32] gradients of the hidden activations
-    float* scal;           // [0] sum of squares, [1] s, [2] 1/s
+    float* scal;           // [0] sum of squares over the shell, [1] its RMS, [2] 1/RMS
+    float* sloc;           // [cell] local scale s(x)
+    float* stmp;           // [cell] box-sum scratch
     float* loss;           // [0] accumulated loss
 };
 
@@ -69,7 +71,7 @@ cudaError_t train_sample(cudaStream_t s, const Net& n, const float2* W, const fl
 // One Adam update with gradients scaled by gscale; clears the gradients.
 cudaError_t adam(cudaStream_t s, const Net& n, float lr, float b1, float b2, float eps, int step, float gscale);
 
-// s = RMS of the state over the shell -> n.scal[1], 1/s -> n.scal[2].
+// Shell RMS -> n.scal[1], 1/RMS -> n.scal[2]; local scale s(x) -> n.sloc.
 cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W);
 void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, std::vector<uint8_t>& out);
 void tc_tiles(const NetGeom& g, std::vector<int>& tiles);

@@ -14,7 +14,7 @@
 //
 // Layer 0's halo is built from the state and the velocity (the 8 features,
 // padded to 16 channels with zeros); hidden activations are BF16 [cell][32];
-// the output layer adds s * (dP, dQ) to the state at the write cells.  Inputs
+// the output layer adds s(x) (dP, dQ) to the state at the write cells.  Inputs
 // outside the shell are zero, as in the FP32 kernels (ose_learn.cu).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -87,7 +87,8 @@ struct LayerCfg {
 
 // MODE 0: layer 0 (features from state + velocity), hidden output (ReLU, BF16)
 // MODE 1: hidden layer, BF16 in, hidden output
-// MODE 2: output layer, BF16 in, state += s * (o0, o1) at the write cells
+// MODE 2: output layer, BF16 in, state += s(x) (o0, o1) at the write cells
+// (scal = the local scale s(x) per cell)
 template <int CIN, int NPAD, int MODE>
 __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict__ act_in,
                                                      const float2* __restrict__ Win, const float* __restrict__ vel,
@@ -112,8 +113,6 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
         for (int i = t; i < C::w_bytes / 16; i += THREADS) d4[i] = s4[i];
         for (int i = t; i < NPAD; i += THREADS) sb[i] = bias[i];
     }
-    const float inv = MODE == 0 ? scal[2] : 0.f;
-    const float sc = MODE == 2 ? scal[1] : 0.f;
     tc5::fence_before_sync();
     __syncthreads();
     tc5::fence_after_sync();
@@ -131,7 +130,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
         constexpr int PER = (UNITS + THREADS - 1) / THREADS;
         if (MODE == 0) {
             float2 wv[PER];
-            float vv[PER];
+            float vv[PER], sv[PER];
             bool ok[PER];
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
@@ -143,6 +142,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
                 const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
                 wv[k] = ok[k] ? __ldg(Win + c) : make_float2(0.f, 0.f);
                 vv[k] = ok[k] ? __ldg(vel + c) : 0.f;
+                sv[k] = ok[k] ? __ldg(scal + c) : 1.f;
             }
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
                 uint4 v = make_uint4(0, 0, 0, 0);
                 if (ok[k]) {
                     const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                    const float inv = 1.f / sv[k];
                     v.x = pack2(wv[k].x * inv, wv[k].y * inv);
                     v.y = pack2(vv[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
                     v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
@@ -213,6 +214,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
             float o[16];
             tc5::tmem_ld16(trow, o);
             if (valid && is_write(g, x, y, z)) {
+                const float sc = scal[c];
                 float2 w = state[c];
                 w.x = fmaf(sc, o[0] + sb[0], w.x);
                 w.y = fmaf(sc, o[1] + sb[1], w.y);
@@ -319,13 +321,13 @@ cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W,
     cudaError_t e = shell_scale(s, n, W);
     if (e != cudaSuccess) return e;
     k_conv_tc<16, 32, 0><<<grid, THREADS, LayerCfg<16, 32>::smem, s>>>(
-        nullptr, W, vel, tc.w[0], tc.b[0], tc.act[0], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+        nullptr, W, vel, tc.w[0], tc.b[0], tc.act[0], nullptr, n.sloc, n.g, tc.tiles, tc.ntiles, tc.err);
     k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
         tc.act[0], nullptr, nullptr, tc.w[1], tc.b[1], tc.act[1], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
     k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
         tc.act[1], nullptr, nullptr, tc.w[2], tc.b[2], tc.act[0], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
     k_conv_tc<32, 16, 2><<<grid, THREADS, LayerCfg<32, 16>::smem, s>>>(
-        tc.act[0], nullptr, nullptr, tc.w[3], tc.b[3], nullptr, W, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+        tc.act[0], nullptr, nullptr, tc.w[3], tc.b[3], nullptr, W, n.sloc, n.g, tc.tiles, tc.ntiles, tc.err);
     return cudaGetLastError();
 }
 

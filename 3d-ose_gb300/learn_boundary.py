@@ -8,7 +8,9 @@ After every step the thin run's state u is paired with the wide run's state
 restricted to the thin grid (the target); then the thin run's interior is
 reset to the wide run's, so the next pair starts from the true interior with
 the thin run's own sponge content.  The network learns the one-step residual
-(target - u) / s on the write cells (the 8 interior cells next to the sponge).
+(target - u) / s(x) on the write cells (the 8 interior cells next to the
+sponge); s(x) is the local RMS of the state (17^3 box), so inputs and targets
+have the same range on any grid size.
 
     python 3d-ose_gb300/learn_boundary.py train --runs 200 --out corrector.npy
     python 3d-ose_gb300/learn_boundary.py eval --weights corrector.npy

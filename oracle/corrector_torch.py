@@ -7,10 +7,13 @@ counterpart in the reference (whose only boundary treatment is the sponge,
 ose_3d_kernel.cu:242-288), so this file restates the network as the library
 defines it:
 
-  features  P/s, Q/s, v/4500, ex, ey, ez, 0, 0   (s = RMS of P, Q over the shell)
+  features  P/s, Q/s, v/4500, ex, ey, ez, 0, 0
+            s = s(x) = sqrt(m/2 + f^2): m the mean of P^2 + Q^2 (shell cells,
+            zero elsewhere) over the periodic 17^3 box around the cell, f =
+            1e-3 x the RMS of P, Q over the shell
   conv 3x3x3 8->32 ReLU, 32->32 ReLU, 32->32 ReLU, 32->2
   periodic grid; every layer's input is zero outside the shell
-  loss = mean over write cells of |out - (target - state)/s|^2
+  loss = mean over write cells of |out - (target - state)/s(x)|^2
 """
 from __future__ import annotations
 
@@ -47,18 +50,28 @@ def face_coord(n: int, shell: int) -> np.ndarray:
     return out
 
 
+def scales(P, Q, shell, sponge6):
+    """(global shell RMS, local scale s(x) [z][y][x])."""
+    from scipy.ndimage import uniform_filter
+    sh, _ = masks(P.shape, shell, sponge6)
+    e = (P ** 2 + Q ** 2) * sh
+    sg = np.sqrt(e.sum() / (2.0 * sh.sum()))
+    m = uniform_filter(e, size=17, mode="wrap")
+    return sg, np.sqrt(0.5 * m + (1e-3 * sg) ** 2)
+
+
 def features(P, Q, vel, shell, sponge6):
-    """[8][z][y][x] features and the scale s."""
+    """[8][z][y][x] features, the global shell RMS and the local scale."""
     nz, ny, nx = P.shape
     sh, _ = masks(P.shape, shell, sponge6)
-    s = np.sqrt(np.sum((P ** 2 + Q ** 2)[sh]) / (2.0 * sh.sum()))
-    inv = 1.0 / s if s > 0 else 0.0
+    s, sl = scales(P, Q, shell, sponge6)
+    inv = 1.0 / sl
     F = np.zeros((8, nz, ny, nx))
     F[0], F[1], F[2] = P * inv, Q * inv, vel / 4500.0
     F[3] = face_coord(nx, shell)[None, None, :]
     F[4] = face_coord(ny, shell)[None, :, None]
     F[5] = face_coord(nz, shell)[:, None, None]
-    return F * sh[None], s
+    return F * sh[None], s, sl
 
 
 def unpack(params, torch):
@@ -88,18 +101,19 @@ def forward(params, F, shell_mask):
 
 
 def loss_and_grads(params_np, P, Q, vel, target_P, target_Q, shell, sponge6):
-    """(loss, d loss / d params as float64 numpy, output [2][z][y][x], s)."""
+    """(loss, d loss / d params as float64 numpy, output [2][z][y][x], global
+    shell RMS, local scale s(x))."""
     import torch
-    F, s = features(P, Q, vel, shell, sponge6)
+    F, s, sl = features(P, Q, vel, shell, sponge6)
     sh, wr = masks(P.shape, shell, sponge6)
     p = torch.tensor(np.asarray(params_np, np.float64), requires_grad=True)
     out = forward(p, torch.as_tensor(F), sh)
-    inv = 1.0 / s if s > 0 else 0.0
+    inv = 1.0 / sl
     r = torch.as_tensor(np.stack([(target_P - P) * inv, (target_Q - Q) * inv]))
     w = torch.as_tensor(wr.astype(np.float64))[None]
     loss = (((out - r) ** 2) * w).sum() / wr.sum()
     loss.backward()
-    return float(loss.detach()), p.grad.numpy().copy(), out.detach().numpy(), s
+    return float(loss.detach()), p.grad.numpy().copy(), out.detach().numpy(), s, sl
 
 
 def init_params(seed: int = 0, scale: float = 1.0) -> np.ndarray:

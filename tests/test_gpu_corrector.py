@@ -55,7 +55,7 @@ def test_forward_and_gradients_match_fp64_autograd():
     params[-2:] = [0.01, -0.02]
     # round-trip the parameters through float32 so both sides use the same values
     p64 = params.astype(np.float64)
-    loss64, g64, out64, s64 = CT.loss_and_grads(p64, P.astype(np.float32).astype(np.float64),
+    loss64, g64, out64, s64, _ = CT.loss_and_grads(p64, P.astype(np.float32).astype(np.float64),
                                                 Q.astype(np.float32).astype(np.float64),
                                                 vel.astype(np.float32).astype(np.float64),
                                                 tP.astype(np.float32).astype(np.float64),
@@ -107,8 +107,11 @@ def test_apply_adds_the_scaled_output_at_write_cells_only():
     after = st.cpu().numpy()
     o = out.cpu().numpy()
     _, wr = CT.masks(SHAPE, SHELL, SPONGE)
+    _, sl = CT.scales(P.astype(np.float32).astype(np.float64), Q.astype(np.float32).astype(np.float64),
+                      SHELL, SPONGE)
     assert np.array_equal(after[~wr], before[~wr])
-    np.testing.assert_allclose(after[wr], before[wr] + s * o[wr], rtol=1e-5, atol=1e-6 * np.abs(before).max())
+    np.testing.assert_allclose(after[wr], before[wr] + sl[wr][:, None] * o[wr], rtol=1e-5,
+                               atol=1e-6 * np.abs(before).max())
 
 
 def test_adam_reduces_the_loss():
