@@ -103,55 +103,67 @@ __global__ void k_shell_scale(float* scal, float inv_count2)
 }
 
 // Local scale s(x): three periodic box sums of P^2 + Q^2 (shell cells) with
-// half-width kBoxR, x then y then z over the whole padded grid.
+// half-width kBoxR, x then y then z over the whole padded grid.  Each thread
+// slides the window along one whole line (one add and one subtract per cell).
 constexpr int kBoxR = 8;
 
+__device__ __forceinline__ int modi(int v, int n) { return ((v % n) + n) % n; }
+
+__device__ __forceinline__ float shell_energy(const float2* __restrict__ W, const NetGeom& g, int x, int y, int z)
+{
+    if (!in_shell(g, x, y, z)) return 0.f;
+    const float2 w = W[((size_t)z * g.ny + y) * g.nx + x];
+    return fmaf(w.x, w.x, w.y * w.y);
+}
+
+// thread per (y, z) row
 __global__ void k_box_x(const float2* __restrict__ W, float* __restrict__ out, NetGeom g)
 {
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % g.nx);
-        const long long row = i - x;
-        const int y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
-        float acc = 0.f;
-        for (int d = -kBoxR; d <= kBoxR; ++d) {
-            const int xn = wrapi(x + d, g.nx);
-            if (in_shell(g, xn, y, z)) {
-                const float2 w = W[row + xn];
-                acc = fmaf(w.x, w.x, fmaf(w.y, w.y, acc));
-            }
-        }
-        out[i] = acc;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= g.ny * g.nz) return;
+    const int y = row % g.ny, z = row / g.ny;
+    float acc = 0.f;
+    for (int d = -kBoxR; d <= kBoxR; ++d) acc += shell_energy(W, g, modi(d, g.nx), y, z);
+    float* o = out + (size_t)row * g.nx;
+    for (int x = 0; x < g.nx; ++x) {
+        o[x] = acc;
+        acc += shell_energy(W, g, modi(x + kBoxR + 1, g.nx), y, z) - shell_energy(W, g, modi(x - kBoxR, g.nx), y, z);
     }
 }
 
+// thread per (x, z) line along y
 __global__ void k_box_y(const float* __restrict__ in, float* __restrict__ out, NetGeom g)
 {
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny);
-        const long long base = i - (long long)y * g.nx;
-        float acc = 0.f;
-        for (int d = -kBoxR; d <= kBoxR; ++d) acc += in[base + (long long)wrapi(y + d, g.ny) * g.nx];
-        out[i] = acc;
-        (void)x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.nx * g.nz) return;
+    const int x = t % g.nx, z = t / g.nx;
+    const float* a = in + (size_t)z * g.ny * g.nx + x;
+    float* o = out + (size_t)z * g.ny * g.nx + x;
+    float acc = 0.f;
+    for (int d = -kBoxR; d <= kBoxR; ++d) acc += a[(size_t)modi(d, g.ny) * g.nx];
+    for (int y = 0; y < g.ny; ++y) {
+        o[(size_t)y * g.nx] = acc;
+        acc += a[(size_t)modi(y + kBoxR + 1, g.ny) * g.nx] - a[(size_t)modi(y - kBoxR, g.ny) * g.nx];
     }
 }
 
-// z sum, then s = sqrt(m / 2 + f^2) with m the box mean and f = 1e-3 s_shell.
+// thread per (x, y) line along z, then s = sqrt(m / 2 + f^2) with m the box
+// mean and f = 1e-3 x the shell RMS.
 __global__ void k_box_z(const float* __restrict__ in, float* __restrict__ sloc, const float* __restrict__ scal,
                         NetGeom g)
 {
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    const long long plane = (long long)g.nx * g.ny;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.nx * g.ny) return;
+    const size_t plane = (size_t)g.nx * g.ny;
     const float f = 1e-3f * scal[1];
     const float inv_vol = 1.f / (float)((2 * kBoxR + 1) * (2 * kBoxR + 1) * (2 * kBoxR + 1));
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int z = (int)(i / plane);
-        const long long base = i - (long long)z * plane;
-        float acc = 0.f;
-        for (int d = -kBoxR; d <= kBoxR; ++d) acc += in[base + (long long)wrapi(z + d, g.nz) * plane];
-        sloc[i] = sqrtf(0.5f * acc * inv_vol + f * f);
+    const float* a = in + t;
+    float* o = sloc + t;
+    float acc = 0.f;
+    for (int d = -kBoxR; d <= kBoxR; ++d) acc += a[(size_t)modi(d, g.nz) * plane];
+    for (int z = 0; z < g.nz; ++z) {
+        o[(size_t)z * plane] = sqrtf(0.5f * fmaxf(acc, 0.f) * inv_vol + f * f);
+        acc += a[(size_t)modi(z + kBoxR + 1, g.nz) * plane] - a[(size_t)modi(z - kBoxR, g.nz) * plane];
     }
 }
 
@@ -499,11 +511,10 @@ cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
     const unsigned gr = grid_for(n.ntiles, 2);
     k_shell_sumsq<<<gr, 256, 0, s>>>(W, n.g, n.tiles, n.ntiles, n.scal);
     k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
-    const long long cells = (long long)n.g.nx * n.g.ny * n.g.nz;
-    const unsigned gb = (unsigned)std::min<long long>(4096, (cells + 255) / 256);
-    k_box_x<<<gb, 256, 0, s>>>(W, n.sloc, n.g);
-    k_box_y<<<gb, 256, 0, s>>>(n.sloc, n.stmp, n.g);
-    k_box_z<<<gb, 256, 0, s>>>(n.stmp, n.sloc, n.scal, n.g);
+    const NetGeom& g = n.g;
+    k_box_x<<<(g.ny * g.nz + 127) / 128, 128, 0, s>>>(W, n.sloc, g);
+    k_box_y<<<(g.nx * g.nz + 127) / 128, 128, 0, s>>>(n.sloc, n.stmp, g);
+    k_box_z<<<(g.nx * g.ny + 127) / 128, 128, 0, s>>>(n.stmp, n.sloc, n.scal, g);
     return cudaGetLastError();
 }
 
