@@ -1,0 +1,282 @@
+// ose_cols.cu - column transforms of the generic path held in registers: the
+// y passes (forward, inverse) and the z pass (forward, * |k|, inverse) for a
+// line length N = 16 C, C in OSE_COL_SIZES (below).
+//
+// A line is a 16 x C matrix (four-step, n = C n1 + j, k = p + 16 k2):
+//   phase 1  thread j < C holds x[C n1 + j], n1 < 16: DFT-16, twiddle W_N^(j p)
+//   transpose through shared memory
+//   phase 2  thread p < 16 holds the j < C values: DFT-C -> X[p + 16 k2]
+// and the inverse runs the same steps backwards.  The DFTs are in registers:
+// DFT-C by compile-time mixed radix (radix 4 first, then the smallest prime
+// factor; direct sums for primes), its twiddles W_N^t from a table in shared
+// memory.  A CTA holds TX neighbouring x columns of one line family, so every
+// global access is a TX-wide row segment.  This replaces the shared-memory
+// Stockham passes (ose_kernels.cu) on these sizes; the x passes stay there.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ose_internal.h"
+
+namespace ose {
+namespace cols {
+
+__host__ __device__ constexpr bool is_prime(int n)
+{
+    if (n < 2) return false;
+    for (int d = 2; d * d <= n; ++d)
+        if (n % d == 0) return false;
+    return true;
+}
+
+__host__ __device__ constexpr int first_factor(int n)
+{
+    if (n % 4 == 0) return 4;
+    for (int d = 2; d <= n; ++d)
+        if (n % d == 0) return d;
+    return n;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+template <bool INV>
+__device__ __forceinline__ float2 tw(const float2* W, int e)
+{
+    const float2 w = W[e];
+    return INV ? make_float2(w.x, -w.y) : w;
+}
+
+// times -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 rot(float2 a)
+{
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// v[0..C) <- DFT_C(v[0..C)) in natural order; W_C^t = W[ST * t] (forward
+// twiddles; conjugated for INV).
+template <int C, int ST, bool INV, int L>
+__device__ __forceinline__ void dftc(float2 (&v)[L], const float2* __restrict__ W)
+{
+    static_assert(C <= L, "array too short");
+    if constexpr (C == 1) {
+    } else if constexpr (C == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if constexpr (C == 4) {
+        const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]), t2 = cadd(v[1], v[3]);
+        const float2 t3 = rot<INV>(csub(v[1], v[3]));
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    } else if constexpr (is_prime(C)) {
+        // direct sums, pairing j and C - j: X_k = x0 + sum_j (x_j + x_{C-j}) cos
+        //                                        -/+ i (x_j - x_{C-j}) sin
+        constexpr int H = (C - 1) / 2;
+        float2 s[H], d[H];
+#pragma unroll
+        for (int j = 1; j <= H; ++j) {
+            s[j - 1] = cadd(v[j], v[C - j]);
+            d[j - 1] = csub(v[j], v[C - j]);
+        }
+        float2 o[C];
+        float2 sum = v[0];
+#pragma unroll
+        for (int j = 0; j < H; ++j) sum = cadd(sum, s[j]);
+        o[0] = sum;
+#pragma unroll
+        for (int k = 1; k <= H; ++k) {
+            float2 re = v[0], im = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 1; j <= H; ++j) {
+                const float2 w = W[ST * ((j * k) % C)];   // (cos, -sin) of 2 pi j k / C
+                re.x = fmaf(s[j - 1].x, w.x, re.x);
+                re.y = fmaf(s[j - 1].y, w.x, re.y);
+                im.x = fmaf(d[j - 1].x, w.y, im.x);
+                im.y = fmaf(d[j - 1].y, w.y, im.y);
+            }
+            // forward: X_k = re + i im_term with im_term = sum d_j (-sin) -> i * (d * w.y)
+            const float2 ii = INV ? make_float2(im.y, -im.x) : make_float2(-im.y, im.x);
+            o[k] = cadd(re, ii);
+            o[C - k] = csub(re, ii);
+        }
+#pragma unroll
+        for (int k = 0; k < C; ++k) v[k] = o[k];
+    } else {
+        constexpr int A = first_factor(C), B = C / A;
+        float2 t[A][B];
+#pragma unroll
+        for (int r = 0; r < A; ++r)
+#pragma unroll
+            for (int m = 0; m < B; ++m) t[r][m] = v[A * m + r];
+#pragma unroll
+        for (int r = 0; r < A; ++r) dftc<B, ST * A, INV, B>(t[r], W);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) {
+            float2 u[A];
+#pragma unroll
+            for (int r = 0; r < A; ++r) u[r] = (r * k2) ? cmul(t[r][k2], tw<INV>(W, ST * r * k2)) : t[r][k2];
+            dftc<A, ST * B, INV, A>(u, W);
+#pragma unroll
+            for (int k1 = 0; k1 < A; ++k1) v[k2 + B * k1] = u[k1];
+        }
+    }
+}
+
+enum { COL_FWD = 0, COL_INV = 1, COL_KSCALE = 2 };
+
+template <int C>
+struct ColCfg {
+    static constexpr int N = 16 * C;
+    static constexpr int P = C > 16 ? C : 16;      // line threads
+    static constexpr int TX = P > 16 ? 8 : 16;     // columns per CTA
+    static constexpr int THREADS = TX * P;
+    static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)N * TX);
+};
+
+// Lines at base + n * stride of the columns x0 .. x0 + TX - 1;
+// blockIdx.y = the other index (z for the y passes, y for the z pass).
+template <int C, int MODE>
+__global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__ X, int nxb, long long stride,
+                                                            long long ostride, const float2* __restrict__ twg,
+                                                            Tables tb)
+{
+    using K = ColCfg<C>;
+    constexpr int N = K::N, TX = K::TX;
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    float2* T = W + N;
+    for (int i = threadIdx.x; i < N; i += K::THREADS) W[i] = twg[i];
+    const int c = threadIdx.x % TX, p = threadIdx.x / TX;
+    const int x = blockIdx.x * TX + c;
+    const bool col_ok = x < nxb;
+    float2* line = X + (size_t)blockIdx.y * ostride + x;
+    __syncthreads();
+
+    if (MODE == COL_FWD || MODE == COL_KSCALE) {
+        if (p < C) {   // phase 1: thread j = p, DFT-16 over n1
+            float2 v[16];
+#pragma unroll
+            for (int n1 = 0; n1 < 16; ++n1) v[n1] = col_ok ? line[(size_t)(C * n1 + p) * stride] : make_float2(0.f, 0.f);
+            dftc<16, C, false>(v, W);
+#pragma unroll
+            for (int k1 = 0; k1 < 16; ++k1) T[(p * 16 + k1) * TX + c] = k1 ? cmul(v[k1], W[p * k1]) : v[k1];
+        }
+        __syncthreads();
+    }
+    float2 u[C];
+    if (p < 16) {
+        if (MODE == COL_INV) {
+#pragma unroll
+            for (int k2 = 0; k2 < C; ++k2) u[k2] = col_ok ? line[(size_t)(p + 16 * k2) * stride] : make_float2(0.f, 0.f);
+        } else {
+#pragma unroll
+            for (int j = 0; j < C; ++j) u[j] = T[(j * 16 + p) * TX + c];
+            dftc<C, 16, false>(u, W);   // u[k2] = X[p + 16 k2]
+        }
+        if (MODE == COL_FWD) {
+            if (col_ok)
+#pragma unroll
+                for (int k2 = 0; k2 < C; ++k2) line[(size_t)(p + 16 * k2) * stride] = u[k2];
+        } else {
+            if (MODE == COL_KSCALE) {
+                // z pass: blockIdx.y is y, x the column
+                const float kxy = col_ok ? __ldg(tb.kx2 + x) + __ldg(tb.ky2 + blockIdx.y) : 0.f;
+#pragma unroll
+                for (int k2 = 0; k2 < C; ++k2) {
+                    const float k = sqrtf(kxy + __ldg(tb.kz2 + p + 16 * k2));
+                    u[k2].x *= k;
+                    u[k2].y *= k;
+                }
+            }
+            dftc<C, 16, true>(u, W);   // u[j] = Z[p][j]
+#pragma unroll
+            for (int j = 0; j < C; ++j) {
+                const float2 w = W[j * p];
+                T[(j * 16 + p) * TX + c] = (j * p) ? cmul(u[j], make_float2(w.x, -w.y)) : u[j];
+            }
+        }
+    }
+    if (MODE == COL_FWD) return;
+    __syncthreads();
+    if (p < C) {   // inverse phase 1: thread j = p, DFT-16 over p'
+        float2 v[16];
+#pragma unroll
+        for (int k1 = 0; k1 < 16; ++k1) v[k1] = T[(p * 16 + k1) * TX + c];
+        dftc<16, C, true>(v, W);
+        if (col_ok)
+#pragma unroll
+            for (int n1 = 0; n1 < 16; ++n1) line[(size_t)(C * n1 + p) * stride] = v[n1];
+    }
+}
+
+template <int C>
+cudaError_t configure_one()
+{
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_col<C, COL_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ColCfg<C>::SMEM)) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_col<C, COL_INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ColCfg<C>::SMEM)) != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_col<C, COL_KSCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ColCfg<C>::SMEM);
+}
+
+template <int C>
+cudaError_t launch_one(cudaStream_t s, int mode, float2* X, int nxb, int nother, long long stride, long long ostride,
+                       const float2* twg, const Tables& t)
+{
+    using K = ColCfg<C>;
+    const dim3 grid((nxb + K::TX - 1) / K::TX, nother);
+    if (mode == COL_FWD) k_col<C, COL_FWD><<<grid, K::THREADS, K::SMEM, s>>>(X, nxb, stride, ostride, twg, t);
+    else if (mode == COL_INV) k_col<C, COL_INV><<<grid, K::THREADS, K::SMEM, s>>>(X, nxb, stride, ostride, twg, t);
+    else k_col<C, COL_KSCALE><<<grid, K::THREADS, K::SMEM, s>>>(X, nxb, stride, ostride, twg, t);
+    return cudaGetLastError();
+}
+
+#define OSE_COL_SIZES(X) X(4) X(6) X(8) X(9) X(10) X(11) X(12) X(16) X(18) X(20) X(23) X(24)
+
+}  // namespace cols
+
+bool col_supported(int n)
+{
+    if (n % 16) return false;
+    switch (n / 16) {
+#define CASE(C) case C:
+        OSE_COL_SIZES(CASE)
+#undef CASE
+        return true;
+    default: return false;
+    }
+}
+
+cudaError_t configure_col_kernels()
+{
+    cudaError_t e = cudaSuccess;
+#define CONF(C) if ((e = cols::configure_one<C>()) != cudaSuccess) return e;
+    OSE_COL_SIZES(CONF)
+#undef CONF
+    return e;
+}
+
+// mode: 0 forward, 1 inverse, 2 forward * |k| inverse (z pass).
+cudaError_t launch_col(cudaStream_t s, int mode, int n, float2* X, int nxb, int nother, long long stride,
+                       long long ostride, const float2* twg, const Tables& t)
+{
+    switch (n / 16) {
+#define LAUNCH(C) case C: return cols::launch_one<C>(s, mode, X, nxb, nother, stride, ostride, twg, t);
+        OSE_COL_SIZES(LAUNCH)
+#undef LAUNCH
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ose

@@ -98,6 +98,12 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
                                   float sch, float scl);
 cudaError_t configure_kernels();
 
+// Register column transforms for lengths 16 C (ose_cols.cu).
+bool col_supported(int n);
+cudaError_t configure_col_kernels();
+cudaError_t launch_col(cudaStream_t s, int mode, int n, float2* X, int nxb, int nother, long long stride,
+                       long long ostride, const float2* twg, const Tables& t);
+
 // 256^3 fast path (ose_plane.cu).
 bool plane_path_supported(int nxb, int nyb, int nzb);
 cudaError_t configure_plane_kernels();

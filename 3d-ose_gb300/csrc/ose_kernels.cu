@@ -18,6 +18,8 @@
 // autosort FFT there (natural order in, natural order out).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "ose_internal.h"
 
@@ -265,7 +267,21 @@ __global__ void __launch_bounds__(kThreads) k_lines(float2* __restrict__ data, G
 }
 
 int rows_per_cta(int n) { return n >= 2048 ? 1 : 2048 / n; }
-int tile_x(int n) { return n <= 640 ? 16 : 8; }
+// 8 columns (64-byte row segments): on 384 x 384 x 256 and 320 x 288 x 256
+// the autotuner of the batched form picks 8 over 16 for both column passes.
+int tile_x(int) { return 8; }
+
+// The register column kernels (ose_cols.cu) where the length allows, unless
+// OSE3D_COLS=stockham asks for the shared-memory Stockham passes (comparison).
+bool use_col_kernels()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("OSE3D_COLS");
+        v = (e && strcmp(e, "stockham") == 0) ? 0 : 1;
+    }
+    return v == 1;
+}
 size_t rows_smem(int n) { return sizeof(float2) * ((size_t)n + 2 * (size_t)rows_per_cta(n) * n); }
 size_t lines_smem(int n) { return sizeof(float2) * ((size_t)n + 2 * (size_t)n * tile_x(n)); }
 
@@ -329,11 +345,19 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
             an, X, g, px, t.twx, rpc, none);
         T.done();
     }
+    const long long plane = (long long)g.nxb * g.nyb;
+    const bool ycols = use_col_kernels() && col_supported(py.n);
+    const bool zcols = use_col_kernels() && col_supported(pz.n);
     {
         Timer T(tm, s, T_YF);
-        const int tx = tile_x(py.n);
-        dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
-        k_lines<false, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        if (ycols) {
+            cudaError_t e = launch_col(s, 0, py.n, X, g.nxb, g.nzb, g.nxb, plane, t.twy, t);
+            if (e != cudaSuccess) return e;
+        } else {
+            const int tx = tile_x(py.n);
+            dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
+            k_lines<false, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        }
         T.done();
     }
     {
@@ -341,19 +365,26 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
         if (t.tcvar != OSE_PRECISION_FP32) {
             cudaError_t e = launch_tensor_zpass(s, X, g, t);
             if (e != cudaSuccess) return e;
+        } else if (zcols) {
+            cudaError_t e = launch_col(s, 2, pz.n, X, g.nxb, g.nyb, plane, g.nxb, t.twz, t);
+            if (e != cudaSuccess) return e;
         } else {
             const int tx = tile_x(pz.n);
             dim3 grid((g.nxb + tx - 1) / tx, g.nyb);
-            k_lines<false, true><<<grid, kThreads, lines_smem(pz.n), s>>>(X, g, pz, t.twz, tx,
-                                                                         (long long)g.nxb * g.nyb, t);
+            k_lines<false, true><<<grid, kThreads, lines_smem(pz.n), s>>>(X, g, pz, t.twz, tx, plane, t);
         }
         T.done();
     }
     {
         Timer T(tm, s, T_YI);
-        const int tx = tile_x(py.n);
-        dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
-        k_lines<true, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        if (ycols) {
+            cudaError_t e = launch_col(s, 1, py.n, X, g.nxb, g.nzb, g.nxb, plane, t.twy, t);
+            if (e != cudaSuccess) return e;
+        } else {
+            const int tx = tile_x(py.n);
+            dim3 grid((g.nxb + tx - 1) / tx, g.nzb);
+            k_lines<true, false><<<grid, kThreads, lines_smem(py.n), s>>>(X, g, py, t.twy, tx, g.nxb, t);
+        }
         T.done();
     }
     return cudaGetLastError();
