@@ -10,11 +10,14 @@
 // DFT-C by compile-time mixed radix (radix 4 first, then the smallest prime
 // factor; direct sums for primes), its twiddles W_N^t from a table in shared
 // memory.  A CTA holds TX neighbouring x columns of one line family, so every
-// global access is a TX-wide row segment.  This replaces the shared-memory
-// Stockham passes (ose_kernels.cu) on these sizes; the x passes stay there.
+// global access is a TX-wide row segment.  The x passes (k_row) use the same
+// two phases on contiguous rows, RW rows per CTA; the inverse x pass ends in
+// the step's pointwise epilogue.  These replace the shared-memory Stockham
+// passes (ose_kernels.cu) on these sizes.
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "ose_epilogue.cuh"
 #include "ose_internal.h"
 
 namespace ose {
@@ -217,6 +220,108 @@ __global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__
 }
 
 template <int C>
+struct RowCfg {
+    static constexpr int N = 16 * C;
+    static constexpr int P = C > 16 ? C : 16;      // line threads
+    static constexpr int RW = P > 16 ? 8 : 16;     // rows per CTA
+    static constexpr int THREADS = RW * P;
+    static constexpr int NP = 17 * C;              // padded row of the transpose buffer
+    static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)RW * NP);
+};
+
+// x rows (contiguous, row = z * nyb + y).  EPI_NONE: forward transform of src
+// into dst.  Otherwise: inverse transform of src followed by epilogue<EPI>.
+template <int C, int EPI>
+__global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
+                                                            int nyb, long long nrows, const float2* __restrict__ twg,
+                                                            EpiArgs e)
+{
+    using K = RowCfg<C>;
+    constexpr int N = K::N, P = K::P, NP = K::NP;
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    float2* T = W + N;
+    for (int i = threadIdx.x; i < N; i += K::THREADS) W[i] = twg[i];
+    const int r = threadIdx.x / P, q = threadIdx.x % P;
+    const long long row = (long long)blockIdx.x * K::RW + r;
+    const bool ok = row < nrows;
+    float2* Tr = T + r * NP;
+    __syncthreads();
+    if (EPI == EPI_NONE) {
+        if (q < C) {   // phase 1: thread j = q, DFT-16 over n1
+            float2 v[16];
+            const float2* in = src + row * N + q;
+#pragma unroll
+            for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? in[C * n1] : make_float2(0.f, 0.f);
+            dftc<16, C, false>(v, W);
+#pragma unroll
+            for (int k1 = 0; k1 < 16; ++k1) Tr[q * 17 + k1] = k1 ? cmul(v[k1], W[q * k1]) : v[k1];
+        }
+        __syncthreads();
+        if (q < 16 && ok) {   // phase 2: thread p = q, DFT-C over j
+            float2 u[C];
+#pragma unroll
+            for (int j = 0; j < C; ++j) u[j] = Tr[j * 17 + q];
+            dftc<C, 16, false>(u, W);
+            float2* out = dst + row * N + q;
+#pragma unroll
+            for (int k2 = 0; k2 < C; ++k2) out[16 * k2] = u[k2];
+        }
+    } else {
+        if (q < 16) {   // inverse phase 2: thread p = q holds X[p + 16 k2]
+            float2 u[C];
+            const float2* in = src + row * N + q;
+#pragma unroll
+            for (int k2 = 0; k2 < C; ++k2) u[k2] = ok ? in[16 * k2] : make_float2(0.f, 0.f);
+            dftc<C, 16, true>(u, W);
+#pragma unroll
+            for (int j = 0; j < C; ++j) {
+                const float2 w = W[j * q];
+                Tr[j * 17 + q] = (j * q) ? cmul(u[j], make_float2(w.x, -w.y)) : u[j];
+            }
+        }
+        __syncthreads();
+        if (q < C && ok) {   // inverse phase 1: thread j = q -> x[C n1 + j]
+            float2 v[16];
+#pragma unroll
+            for (int k1 = 0; k1 < 16; ++k1) v[k1] = Tr[q * 17 + k1];
+            dftc<16, C, true>(v, W);
+            const int y = (int)(row % nyb), z = (int)(row / nyb);
+#pragma unroll
+            for (int n1 = 0; n1 < 16; ++n1) {
+                const int x = C * n1 + q;
+                epilogue<EPI>(row * N + x, x, y, z, v[n1], e);
+            }
+        }
+    }
+}
+
+template <int C, int EPI>
+cudaError_t launch_row_one(cudaStream_t s, const float2* src, float2* dst, int nyb, long long nrows,
+                           const float2* twg, const EpiArgs& e)
+{
+    using K = RowCfg<C>;
+    const unsigned grid = (unsigned)((nrows + K::RW - 1) / K::RW);
+    k_row<C, EPI><<<grid, K::THREADS, K::SMEM, s>>>(src, dst, nyb, nrows, twg, e);
+    return cudaGetLastError();
+}
+
+template <int C>
+cudaError_t launch_row_c(cudaStream_t s, int epi, const float2* src, float2* dst, int nyb, long long nrows,
+                         const float2* twg, const EpiArgs& e)
+{
+    switch (epi) {
+    case EPI_NONE: return launch_row_one<C, EPI_NONE>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_FIRST: return launch_row_one<C, EPI_FIRST>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_MID: return launch_row_one<C, EPI_MID>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_LAST: return launch_row_one<C, EPI_LAST>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_SCALE: return launch_row_one<C, EPI_SCALE>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_SCALE_VEL: return launch_row_one<C, EPI_SCALE_VEL>(s, src, dst, nyb, nrows, twg, e);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int C>
 cudaError_t configure_one()
 {
     cudaError_t e;
@@ -265,6 +370,19 @@ cudaError_t configure_col_kernels()
     OSE_COL_SIZES(CONF)
 #undef CONF
     return e;
+}
+
+// x rows of length n: epi = EPI_NONE forward src -> dst, else inverse of src
+// and the epilogue.
+cudaError_t launch_row(cudaStream_t s, int epi, int n, const float2* src, float2* dst, int nyb, long long nrows,
+                       const float2* twg, const EpiArgs& e)
+{
+    switch (n / 16) {
+#define LAUNCH(C) case C: return cols::launch_row_c<C>(s, epi, src, dst, nyb, nrows, twg, e);
+        OSE_COL_SIZES(LAUNCH)
+#undef LAUNCH
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 // mode: 0 forward, 1 inverse, 2 forward * |k| inverse (z pass).

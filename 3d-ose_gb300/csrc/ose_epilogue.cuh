@@ -1,0 +1,66 @@
+// ose_epilogue.cuh - the pointwise work of one operator application, shared
+// by the shared-memory row kernels (ose_kernels.cu) and the register row
+// kernels (ose_cols.cu): scal_vr_3d, the recurrence, add_bessel_3d,
+// apply_ABC_Xt and the receiver row of ose_3d_lib.cu:651-874, fused.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ose_internal.h"
+
+namespace ose {
+
+// EPI_SCALE_VEL: out = X * vel[i] * scale (the allocation-free entry point)
+enum { EPI_NONE = -1, EPI_SCALE_VEL = 4 };
+
+// The pointwise work of one application on cell i = (x, y, z); X is the
+// unnormalised inverse transform, e.vs the velocity, (e.sch + e.scl) = 1/(R N).
+template <int EPI>
+__device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float2 X, const EpiArgs& e)
+{
+    const float v = __ldg(e.vs + i);
+    float2 Lx = make_float2(X.x * v, X.y * v);
+    // compensated: vs holds v and (sch + scl) = 1/(R N); else vs holds v/(R N)
+    if (kCompensatedConstants || EPI == EPI_SCALE_VEL)
+        Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
+    if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
+        e.prev[i] = Lx;
+    } else if (EPI == EPI_FIRST) {
+        // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1   (ose_3d_lib.cu:651-744)
+        const float2 a1 = make_float2(Lx.y, -Lx.x);
+        const float2 w = e.w[i];
+        e.prev[i] = a1;
+        if (kCompensatedConstants)
+            e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
+                                 fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
+        else
+            e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+    } else {
+        // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
+        const float2 am = e.prev[i];
+        const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
+        const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
+        float2 s = e.S[i];
+        if (kCompensatedConstants) {
+            s.x = fmaf(e.c1l, an.x, s.x);
+            s.y = fmaf(e.c1l, an.y, s.y);
+        }
+        s.x = fmaf(e.c1, an.x, s.x) * att;
+        s.y = fmaf(e.c1, an.y, s.y) * att;
+        if (EPI == EPI_MID) {
+            e.prev[i] = an;
+            e.S[i] = s;
+        } else {
+            e.wout[i] = s;
+            if (z == e.gz) {
+                const int ix = x - e.bl, iy = y - e.bf;
+                if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
+                    const int c = *e.cur;
+                    if (c >= 0 && c < e.nt) e.gather[(long long)c * e.nx * e.ny + iy * e.nx + ix] = s.y;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace ose

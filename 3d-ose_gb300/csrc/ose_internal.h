@@ -103,6 +103,9 @@ bool col_supported(int n);
 cudaError_t configure_col_kernels();
 cudaError_t launch_col(cudaStream_t s, int mode, int n, float2* X, int nxb, int nother, long long stride,
                        long long ostride, const float2* twg, const Tables& t);
+// epi: -1 = forward src -> dst, else an EpiMode (or 4 = scale by a velocity array)
+cudaError_t launch_row(cudaStream_t s, int epi, int n, const float2* src, float2* dst, int nyb, long long nrows,
+                       const float2* twg, const EpiArgs& e);
 
 // 256^3 fast path (ose_plane.cu).
 bool plane_path_supported(int nxb, int nyb, int nzb);

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include "ose_internal.h"
+#include "ose_epilogue.cuh"
 
 namespace ose {
 
@@ -129,59 +130,6 @@ __device__ float2* fft_lines(float2* a, float2* b, int L, int LS, int ES, bool l
         float2* t = a; a = b; b = t;
     }
     return a;
-}
-
-// EPI_SCALE_VEL: out = X * vel[i] * scale (the allocation-free entry point)
-enum { EPI_NONE = -1, EPI_SCALE_VEL = 4 };
-
-// The pointwise work of one application on cell i = (x, y, z); X is the
-// unnormalised inverse transform, e.vs the velocity, (e.sch + e.scl) = 1/(R N).
-template <int EPI>
-__device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float2 X, const EpiArgs& e)
-{
-    const float v = __ldg(e.vs + i);
-    float2 Lx = cscale(X, v);
-    // compensated: vs holds v and (sch + scl) = 1/(R N); else vs holds v/(R N)
-    if (kCompensatedConstants || EPI == EPI_SCALE_VEL)
-        Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
-    if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
-        e.prev[i] = Lx;
-    } else if (EPI == EPI_FIRST) {
-        // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1   (ose_3d_lib.cu:651-744)
-        const float2 a1 = make_float2(Lx.y, -Lx.x);
-        const float2 w = e.w[i];
-        e.prev[i] = a1;
-        if (kCompensatedConstants)
-            e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
-                                 fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
-        else
-            e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
-    } else {
-        // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
-        const float2 am = e.prev[i];
-        const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
-        const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
-        float2 s = e.S[i];
-        if (kCompensatedConstants) {
-            s.x = fmaf(e.c1l, an.x, s.x);
-            s.y = fmaf(e.c1l, an.y, s.y);
-        }
-        s.x = fmaf(e.c1, an.x, s.x) * att;
-        s.y = fmaf(e.c1, an.y, s.y) * att;
-        if (EPI == EPI_MID) {
-            e.prev[i] = an;
-            e.S[i] = s;
-        } else {
-            e.wout[i] = s;
-            if (z == e.gz) {
-                const int ix = x - e.bl, iy = y - e.bf;
-                if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
-                    const int c = *e.cur;
-                    if (c >= 0 && c < e.nt) e.gather[(long long)c * e.nx * e.ny + iy * e.nx + ix] = s.y;
-                }
-            }
-        }
-    }
 }
 
 // Pass over x rows: rows_per_cta consecutive rows (one contiguous block).
@@ -340,9 +288,14 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     const long long nrows = (long long)g.nyb * g.nzb;
     {
         Timer T(tm, s, T_XF);
-        const int rpc = rows_per_cta(px.n);
-        k_rows<false, EPI_NONE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
-            an, X, g, px, t.twx, rpc, none);
+        if (use_col_kernels() && col_supported(px.n)) {
+            cudaError_t e = launch_row(s, EPI_NONE, px.n, an, X, g.nyb, nrows, t.twx, none);
+            if (e != cudaSuccess) return e;
+        } else {
+            const int rpc = rows_per_cta(px.n);
+            k_rows<false, EPI_NONE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
+                an, X, g, px, t.twx, rpc, none);
+        }
         T.done();
     }
     const long long plane = (long long)g.nxb * g.nyb;
@@ -401,6 +354,11 @@ cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const 
     const int rpc = rows_per_cta(px.n);
     const unsigned nb = (unsigned)((nrows + rpc - 1) / rpc);
     Timer T(tm, s, T_XI);
+    if (use_col_kernels() && col_supported(px.n)) {
+        err = launch_row(s, (int)mode, px.n, X, nullptr, g.nyb, nrows, t.twx, e);
+        T.done();
+        return err;
+    }
     switch (mode) {
     case EPI_FIRST:
         k_rows<true, EPI_FIRST><<<nb, kThreads, rows_smem(px.n), s>>>(X, nullptr, g, px, t.twx, rpc, e);
@@ -429,6 +387,7 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
     e.sch = sch;
     e.scl = scl;
     const long long nrows = (long long)g.nyb * g.nzb;
+    if (use_col_kernels() && col_supported(px.n)) return launch_row(s, EPI_SCALE, px.n, X, nullptr, g.nyb, nrows, t.twx, e);
     const int rpc = rows_per_cta(px.n);
     k_rows<true, EPI_SCALE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
         X, nullptr, g, px, t.twx, rpc, e);
@@ -656,6 +615,8 @@ cudaError_t launch_apply_operator_vel(cudaStream_t s, const Geometry& g, const A
     e.vs = vel;
     split_float(scale, &e.sch, &e.scl);
     const long long nrows = (long long)g.nyb * g.nzb;
+    if (use_col_kernels() && col_supported(px.n))
+        return launch_row(s, EPI_SCALE_VEL, px.n, X, nullptr, g.nyb, nrows, t.twx, e);
     const int rpc = rows_per_cta(px.n);
     k_rows<true, EPI_SCALE_VEL><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
         X, nullptr, g, px, t.twx, rpc, e);
