@@ -43,7 +43,8 @@ struct ose_batch {
     ose::BatchShot* d_shots = nullptr;
     int2* d_work = nullptr;
     size_t work_cap = 0;
-    std::vector<ose::BatchPass> passes;    // 3 per application n (rows, y lines, z lines)
+    std::vector<ose::BatchPass> passes;    // every pass of every application, in launch order
+    std::vector<int> pass_begin;           // passes of application n: [pass_begin[n], pass_begin[n + 1])
     char* arena = nullptr;
     size_t arena_bytes = 0;
     cudaStream_t stream = nullptr;
@@ -97,38 +98,64 @@ void fill_descriptors(ose_batch* b)
     }
 }
 
-// Work lists and shared-memory sizes of every application n.
+// Work lists of every application n: five passes (x forward, y forward,
+// z, y inverse, x inverse + update), each split by the axis length of the
+// shots: one launch per length the register kernels have (ose_cols.cu), one
+// launch of the Stockham kernels for all other lengths.
 ose_status build_passes(ose_batch* b)
 {
     std::vector<int2> all;
-    std::vector<std::pair<size_t, size_t>> ranges;   // (offset, count) per pass
-    std::vector<size_t> smem;
+    struct Range { size_t off, count, smem; int kind, n_axis; };
+    std::vector<Range> ranges;
+    std::vector<int> begin;
     b->passes.clear();
     for (int n = 0; n <= b->Mmax; ++n) {
-        for (int kind = 0; kind < 3; ++kind) {
-            const size_t off = all.size();
-            size_t sm = 0;
+        begin.push_back((int)ranges.size());
+        for (int kind = 0; kind < 5; ++kind) {
+            auto axis_len = [&](const ose::BatchShot& D) {
+                return kind == 0 || kind == 4 ? D.g.nxb : (kind == 2 ? D.g.nzb : D.g.nyb);
+            };
+            std::vector<int> lens;   // register classes present, then 0 = Stockham
             for (int s = 0; s < b->nshots; ++s) {
                 const ose::BatchShot& D = b->desc[s];
                 if (D.M < n) continue;
-                int nb;
-                if (kind == 0) {
-                    nb = (int)(((long long)D.g.nyb * D.g.nzb + D.rpc - 1) / D.rpc);
-                    sm = std::max(sm, ose::batch_rows_smem(D.g.nxb, D.rpc));
-                } else if (kind == 1) {
-                    nb = (D.g.nxb + D.txy - 1) / D.txy * D.g.nzb;
-                    sm = std::max(sm, ose::batch_lines_smem(D.g.nyb, D.txy));
-                } else {
-                    nb = (D.g.nxb + D.txz - 1) / D.txz * D.g.nyb;
-                    sm = std::max(sm, ose::batch_lines_smem(D.g.nzb, D.txz));
-                }
-                for (int k = 0; k < nb; ++k) all.push_back(make_int2(s, k));
+                const int L = ose::col_supported(axis_len(D)) ? axis_len(D) : 0;
+                if (std::find(lens.begin(), lens.end(), L) == lens.end()) lens.push_back(L);
             }
-            if (sm > 227 * 1024) return bfail(b, OSE_ERR_UNSUPPORTED, "a tile does not fit shared memory");
-            ranges.push_back({off, all.size() - off});
-            smem.push_back(sm);
+            std::sort(lens.begin(), lens.end(), [](int a, int c) { return a > c; });
+            for (int L : lens) {
+                const size_t off = all.size();
+                size_t sm = 0;
+                for (int s = 0; s < b->nshots; ++s) {
+                    const ose::BatchShot& D = b->desc[s];
+                    if (D.M < n) continue;
+                    const int len = axis_len(D);
+                    if ((ose::col_supported(len) ? len : 0) != L) continue;
+                    long long nb;
+                    if (L > 0) {
+                        if (kind == 0 || kind == 4)
+                            nb = ((long long)D.g.nyb * D.g.nzb + ose::row_tile(L) - 1) / ose::row_tile(L);
+                        else
+                            nb = (long long)((D.g.nxb + ose::col_tile(L) - 1) / ose::col_tile(L)) *
+                                 (kind == 2 ? D.g.nyb : D.g.nzb);
+                    } else if (kind == 0 || kind == 4) {
+                        nb = ((long long)D.g.nyb * D.g.nzb + D.rpc - 1) / D.rpc;
+                        sm = std::max(sm, ose::batch_rows_smem(D.g.nxb, D.rpc));
+                    } else if (kind == 2) {
+                        nb = (long long)(D.g.nxb + D.txz - 1) / D.txz * D.g.nyb;
+                        sm = std::max(sm, ose::batch_lines_smem(D.g.nzb, D.txz));
+                    } else {
+                        nb = (long long)(D.g.nxb + D.txy - 1) / D.txy * D.g.nzb;
+                        sm = std::max(sm, ose::batch_lines_smem(D.g.nyb, D.txy));
+                    }
+                    for (long long k = 0; k < nb; ++k) all.push_back(make_int2(s, (int)k));
+                }
+                if (sm > 227 * 1024) return bfail(b, OSE_ERR_UNSUPPORTED, "a tile does not fit shared memory");
+                ranges.push_back({off, all.size() - off, sm, kind, L});
+            }
         }
     }
+    begin.push_back((int)ranges.size());
     if (all.size() > b->work_cap) {
         if (b->d_work) cudaFree(b->d_work);
         b->d_work = nullptr;
@@ -139,8 +166,9 @@ ose_status build_passes(ose_batch* b)
     BCK(b, cudaMemcpyAsync(b->d_shots, b->desc.data(), sizeof(ose::BatchShot) * b->nshots,
                            cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
-    for (size_t i = 0; i < ranges.size(); ++i)
-        b->passes.push_back({b->d_work + ranges[i].first, (int)ranges[i].second, smem[i]});
+    for (const Range& r : ranges)
+        b->passes.push_back({b->d_work + r.off, (int)r.count, r.smem, r.kind, r.n_axis});
+    b->pass_begin = begin;
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     return OSE_OK;
 }
@@ -150,9 +178,13 @@ cudaError_t enqueue_batch_step(ose_batch* b)
     cudaError_t e = ose::launch_batch_inject(b->stream, b->d_shots, b->nshots);
     if (e != cudaSuccess) return e;
     for (int n = 0; n <= b->Mmax; ++n) {
-        e = ose::launch_batch_application(b->stream, b->d_shots, n, b->passes[3 * n], b->passes[3 * n + 1],
-                                          b->passes[3 * n + 2]);
-        if (e != cudaSuccess) return e;
+        for (int i = b->pass_begin[n]; i < b->pass_begin[n + 1]; ++i) {
+            const ose::BatchPass& p = b->passes[i];
+            e = p.n_axis > 0 ? ose::launch_batch_col_pass(b->stream, p.kind, p.n_axis, b->d_shots, p.work,
+                                                          p.nblocks, n)
+                             : ose::launch_batch_stockham_pass(b->stream, b->d_shots, n, p);
+            if (e != cudaSuccess) return e;
+        }
     }
     return cudaSuccess;
 }

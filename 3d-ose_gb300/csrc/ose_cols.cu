@@ -143,23 +143,22 @@ struct ColCfg {
     static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)N * TX);
 };
 
-// Lines at base + n * stride of the columns x0 .. x0 + TX - 1;
-// blockIdx.y = the other index (z for the y passes, y for the z pass).
+// Lines at base + n * stride of the columns x0 .. x0 + TX - 1 (x tile xt);
+// `other` = the other index (z for the y passes, y for the z pass).
+// W: shared twiddle table (N), T: shared transpose buffer (N x TX).
 template <int C, int MODE>
-__global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__ X, int nxb, long long stride,
-                                                            long long ostride, const float2* __restrict__ twg,
-                                                            Tables tb)
+__device__ __forceinline__ void col_body(float2* __restrict__ X, int nxb, long long stride, long long ostride,
+                                         const float2* __restrict__ twg, const float* __restrict__ kx2,
+                                         const float* __restrict__ ky2, const float* __restrict__ kz2, int xt,
+                                         int other, float2* W, float2* T)
 {
     using K = ColCfg<C>;
     constexpr int N = K::N, TX = K::TX;
-    extern __shared__ float4 smem4[];
-    float2* W = reinterpret_cast<float2*>(smem4);
-    float2* T = W + N;
     for (int i = threadIdx.x; i < N; i += K::THREADS) W[i] = twg[i];
     const int c = threadIdx.x % TX, p = threadIdx.x / TX;
-    const int x = blockIdx.x * TX + c;
+    const int x = xt * TX + c;
     const bool col_ok = x < nxb;
-    float2* line = X + (size_t)blockIdx.y * ostride + x;
+    float2* line = X + (size_t)other * ostride + x;
     __syncthreads();
 
     if (MODE == COL_FWD || MODE == COL_KSCALE) {
@@ -189,11 +188,11 @@ __global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__
                 for (int k2 = 0; k2 < C; ++k2) line[(size_t)(p + 16 * k2) * stride] = u[k2];
         } else {
             if (MODE == COL_KSCALE) {
-                // z pass: blockIdx.y is y, x the column
-                const float kxy = col_ok ? __ldg(tb.kx2 + x) + __ldg(tb.ky2 + blockIdx.y) : 0.f;
+                // z pass: other is y, x the column
+                const float kxy = col_ok ? __ldg(kx2 + x) + __ldg(ky2 + other) : 0.f;
 #pragma unroll
                 for (int k2 = 0; k2 < C; ++k2) {
-                    const float k = sqrtf(kxy + __ldg(tb.kz2 + p + 16 * k2));
+                    const float k = sqrtf(kxy + __ldg(kz2 + p + 16 * k2));
                     u[k2].x *= k;
                     u[k2].y *= k;
                 }
@@ -219,6 +218,36 @@ __global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__
     }
 }
 
+template <int C, int MODE>
+__global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__ X, int nxb, long long stride,
+                                                            long long ostride, const float2* __restrict__ twg,
+                                                            Tables tb)
+{
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    col_body<C, MODE>(X, nxb, stride, ostride, twg, tb.kx2, tb.ky2, tb.kz2, blockIdx.x, blockIdx.y, W,
+                      W + ColCfg<C>::N);
+}
+
+// Batched: CTA b works on block work[b].y = x tile + (x tiles) * other of
+// shot work[b].x; AXIS 1 = y lines, 2 = z lines.
+template <int C, int MODE, int AXIS>
+__global__ void __launch_bounds__(ColCfg<C>::THREADS) kb_col(const BatchShot* __restrict__ shots,
+                                                             const int2* __restrict__ work)
+{
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    const int2 wk = work[blockIdx.x];
+    const BatchShot& S = shots[wk.x];
+    const int ntx = (S.g.nxb + ColCfg<C>::TX - 1) / ColCfg<C>::TX;
+    const int xt = wk.y % ntx, other = wk.y / ntx;
+    const long long plane = (long long)S.g.nxb * S.g.nyb;
+    if (AXIS == 1)
+        col_body<C, MODE>(S.X, S.g.nxb, S.g.nxb, plane, S.twy, S.kx2, S.ky2, S.kz2, xt, other, W, W + ColCfg<C>::N);
+    else
+        col_body<C, MODE>(S.X, S.g.nxb, plane, S.g.nxb, S.twz, S.kx2, S.ky2, S.kz2, xt, other, W, W + ColCfg<C>::N);
+}
+
 template <int C>
 struct RowCfg {
     static constexpr int N = 16 * C;
@@ -229,21 +258,19 @@ struct RowCfg {
     static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)RW * NP);
 };
 
-// x rows (contiguous, row = z * nyb + y).  EPI_NONE: forward transform of src
-// into dst.  Otherwise: inverse transform of src followed by epilogue<EPI>.
+// x rows (contiguous, row = z * nyb + y) of row block rb.  EPI_NONE: forward
+// transform of src into dst.  Otherwise: inverse transform of src followed by
+// epilogue<EPI>.
 template <int C, int EPI>
-__global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
-                                                            int nyb, long long nrows, const float2* __restrict__ twg,
-                                                            EpiArgs e)
+__device__ __forceinline__ void row_body(const float2* __restrict__ src, float2* __restrict__ dst, int nyb,
+                                         long long nrows, const float2* __restrict__ twg, const EpiArgs& e,
+                                         long long rb, float2* W, float2* T)
 {
     using K = RowCfg<C>;
     constexpr int N = K::N, P = K::P, NP = K::NP;
-    extern __shared__ float4 smem4[];
-    float2* W = reinterpret_cast<float2*>(smem4);
-    float2* T = W + N;
     for (int i = threadIdx.x; i < N; i += K::THREADS) W[i] = twg[i];
     const int r = threadIdx.x / P, q = threadIdx.x % P;
-    const long long row = (long long)blockIdx.x * K::RW + r;
+    const long long row = rb * K::RW + r;
     const bool ok = row < nrows;
     float2* Tr = T + r * NP;
     __syncthreads();
@@ -297,6 +324,39 @@ __global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __rest
 }
 
 template <int C, int EPI>
+__global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
+                                                            int nyb, long long nrows, const float2* __restrict__ twg,
+                                                            EpiArgs e)
+{
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    row_body<C, EPI>(src, dst, nyb, nrows, twg, e, blockIdx.x, W, W + RowCfg<C>::N);
+}
+
+// Batched x rows of application n: forward (a_n -> X) or inverse + the series
+// update (FIRST, MID or LAST by the shot's series order M).
+template <int C, bool INV>
+__global__ void __launch_bounds__(RowCfg<C>::THREADS) kb_row(const BatchShot* __restrict__ shots,
+                                                             const int2* __restrict__ work, int n)
+{
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    float2* T = W + RowCfg<C>::N;
+    const int2 wk = work[blockIdx.x];
+    const BatchShot& S = shots[wk.x];
+    const long long nrows = (long long)S.g.nyb * S.g.nzb;
+    if (!INV) {
+        const float2* src = n == 0 ? S.W : ((n & 1) ? S.A : S.W);
+        row_body<C, EPI_NONE>(src, S.X, S.g.nyb, nrows, S.twx, EpiArgs{}, wk.y, W, T);
+        return;
+    }
+    const EpiArgs e = batch_epi(S, n);
+    if (n == 0) row_body<C, EPI_FIRST>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+    else if (n == S.M) row_body<C, EPI_LAST>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+    else row_body<C, EPI_MID>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+}
+
+template <int C, int EPI>
 cudaError_t launch_row_one(cudaStream_t s, const float2* src, float2* dst, int nyb, long long nrows,
                            const float2* twg, const EpiArgs& e)
 {
@@ -347,7 +407,21 @@ cudaError_t launch_one(cudaStream_t s, int mode, float2* X, int nxb, int nother,
     return cudaGetLastError();
 }
 
-#define OSE_COL_SIZES(X) X(4) X(6) X(8) X(9) X(10) X(11) X(12) X(16) X(18) X(20) X(23) X(24)
+#define OSE_COL_SIZES(X) X(4) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(16) X(18) X(20) X(23) X(24)
+
+template <int C>
+cudaError_t launch_batch_one(cudaStream_t s, int kind, const BatchShot* shots, const int2* work, int nblocks, int n)
+{
+    if (nblocks <= 0) return cudaSuccess;
+    switch (kind) {
+    case 0: kb_row<C, false><<<nblocks, RowCfg<C>::THREADS, RowCfg<C>::SMEM, s>>>(shots, work, n); break;
+    case 1: kb_col<C, COL_FWD, 1><<<nblocks, ColCfg<C>::THREADS, ColCfg<C>::SMEM, s>>>(shots, work); break;
+    case 2: kb_col<C, COL_KSCALE, 2><<<nblocks, ColCfg<C>::THREADS, ColCfg<C>::SMEM, s>>>(shots, work); break;
+    case 3: kb_col<C, COL_INV, 1><<<nblocks, ColCfg<C>::THREADS, ColCfg<C>::SMEM, s>>>(shots, work); break;
+    default: kb_row<C, true><<<nblocks, RowCfg<C>::THREADS, RowCfg<C>::SMEM, s>>>(shots, work, n); break;
+    }
+    return cudaGetLastError();
+}
 
 }  // namespace cols
 
@@ -371,6 +445,23 @@ cudaError_t configure_col_kernels()
 #undef CONF
     return e;
 }
+
+// Batched pass `kind` (0 x forward, 1 y forward, 2 z, 3 y inverse, 4 x inverse +
+// update) of application n over the blocks of the shots whose length on that
+// axis is n_axis = 16 C.
+cudaError_t launch_batch_col_pass(cudaStream_t s, int kind, int n_axis, const BatchShot* shots, const int2* work,
+                                  int nblocks, int n)
+{
+    switch (n_axis / 16) {
+#define LAUNCH(C) case C: return cols::launch_batch_one<C>(s, kind, shots, work, nblocks, n);
+        OSE_COL_SIZES(LAUNCH)
+#undef LAUNCH
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+int col_tile(int n_axis) { return n_axis / 16 > 16 ? 8 : 16; }
+int row_tile(int n_axis) { return n_axis / 16 > 16 ? 8 : 16; }
 
 // x rows of length n: epi = EPI_NONE forward src -> dst, else inverse of src
 // and the epilogue.

@@ -63,4 +63,33 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
     }
 }
 
+// The epilogue arguments of batched shot S at application n.
+__device__ __forceinline__ EpiArgs batch_epi(const BatchShot& S, int n)
+{
+    EpiArgs e{};
+    e.vs = S.vs;
+    e.ax = S.ax;
+    e.ay = S.ay;
+    e.az = S.az;
+    e.S = S.S;
+    e.wout = S.W;
+    e.w = S.W;
+    e.prev = n == 0 ? S.A : ((n & 1) ? S.W : S.A);
+    e.sch = S.sch;
+    e.scl = S.scl;
+    e.c0 = S.c0;
+    e.c0l = S.c0l;
+    e.c1 = S.c[n];
+    e.c1l = S.cl[n];
+    e.gather = S.gather;
+    e.cur = S.ctr + 1;
+    e.gz = S.gz;
+    e.bl = S.bl;
+    e.bf = S.bf;
+    e.nx = S.nx;
+    e.ny = S.ny;
+    e.nt = S.nt;
+    return e;
+}
+
 }  // namespace ose

@@ -98,11 +98,20 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
                                   float sch, float scl);
 cudaError_t configure_kernels();
 
+struct BatchShot;
+
 // Register column transforms for lengths 16 C (ose_cols.cu).
 bool col_supported(int n);
 cudaError_t configure_col_kernels();
 cudaError_t launch_col(cudaStream_t s, int mode, int n, float2* X, int nxb, int nother, long long stride,
                        long long ostride, const float2* twg, const Tables& t);
+// Batched register passes (kind 0 x fwd, 1 y fwd, 2 z, 3 y inv, 4 x inv + update)
+// over the shots whose axis length is n_axis; x tile of the column passes
+// and rows per CTA of the row passes for that length.
+cudaError_t launch_batch_col_pass(cudaStream_t s, int kind, int n_axis, const BatchShot* shots, const int2* work,
+                                  int nblocks, int n);
+int col_tile(int n_axis);
+int row_tile(int n_axis);
 // epi: -1 = forward src -> dst, else an EpiMode (or 4 = scale by a velocity array)
 cudaError_t launch_row(cudaStream_t s, int epi, int n, const float2* src, float2* dst, int nyb, long long nrows,
                        const float2* twg, const EpiArgs& e);
@@ -150,17 +159,21 @@ struct BatchShot {
 };
 
 // One batched pass: work[b] = (shot, block of that shot), b < nblocks.
+// kind: 0 x forward, 1 y forward, 2 z (forward * |k| inverse), 3 y inverse,
+// 4 x inverse + series update.  n_axis > 0: the register kernels for that
+// axis length (ose_cols.cu); 0: the shared-memory Stockham kernels.
 struct BatchPass {
     const int2* work;
     int nblocks;
     size_t smem;
+    int kind;
+    int n_axis;
 };
 
 cudaError_t configure_batch_kernels();
 cudaError_t launch_batch_inject(cudaStream_t s, const BatchShot* shots, int nshots);
-// One operator application n for every shot with M >= n: five batched passes.
-cudaError_t launch_batch_application(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& rows,
-                                     const BatchPass& ylines, const BatchPass& zlines);
+// One pass of operator application n (shared-memory Stockham kernels).
+cudaError_t launch_batch_stockham_pass(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& p);
 size_t batch_rows_smem(int n, int rpc);
 size_t batch_lines_smem(int n, int tx);
 

@@ -426,34 +426,6 @@ cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float*
 
 namespace {
 
-__device__ EpiArgs batch_epi(const BatchShot& S, int n)
-{
-    EpiArgs e{};
-    e.vs = S.vs;
-    e.ax = S.ax;
-    e.ay = S.ay;
-    e.az = S.az;
-    e.S = S.S;
-    e.wout = S.W;
-    e.w = S.W;
-    e.prev = n == 0 ? S.A : ((n & 1) ? S.W : S.A);
-    e.sch = S.sch;
-    e.scl = S.scl;
-    e.c0 = S.c0;
-    e.c0l = S.c0l;
-    e.c1 = S.c[n];
-    e.c1l = S.cl[n];
-    e.gather = S.gather;
-    e.cur = S.ctr + 1;
-    e.gz = S.gz;
-    e.bl = S.bl;
-    e.bf = S.bf;
-    e.nx = S.nx;
-    e.ny = S.ny;
-    e.nt = S.nt;
-    return e;
-}
-
 // x rows of application n: forward (a_n -> X) or inverse + the series update.
 template <bool INV>
 __global__ void __launch_bounds__(kThreads) kb_rows(const BatchShot* __restrict__ shots,
@@ -588,15 +560,16 @@ cudaError_t launch_batch_inject(cudaStream_t s, const BatchShot* shots, int nsho
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_application(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& rows,
-                                     const BatchPass& ylines, const BatchPass& zlines)
+cudaError_t launch_batch_stockham_pass(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& p)
 {
-    if (rows.nblocks == 0) return cudaSuccess;
-    kb_rows<false><<<rows.nblocks, kThreads, rows.smem, s>>>(shots, rows.work, n);
-    kb_lines<1, false><<<ylines.nblocks, kThreads, ylines.smem, s>>>(shots, ylines.work);
-    kb_lines<2, false><<<zlines.nblocks, kThreads, zlines.smem, s>>>(shots, zlines.work);
-    kb_lines<1, true><<<ylines.nblocks, kThreads, ylines.smem, s>>>(shots, ylines.work);
-    kb_rows<true><<<rows.nblocks, kThreads, rows.smem, s>>>(shots, rows.work, n);
+    if (p.nblocks <= 0) return cudaSuccess;
+    switch (p.kind) {
+    case 0: kb_rows<false><<<p.nblocks, kThreads, p.smem, s>>>(shots, p.work, n); break;
+    case 1: kb_lines<1, false><<<p.nblocks, kThreads, p.smem, s>>>(shots, p.work); break;
+    case 2: kb_lines<2, false><<<p.nblocks, kThreads, p.smem, s>>>(shots, p.work); break;
+    case 3: kb_lines<1, true><<<p.nblocks, kThreads, p.smem, s>>>(shots, p.work); break;
+    default: kb_rows<true><<<p.nblocks, kThreads, p.smem, s>>>(shots, p.work, n); break;
+    }
     return cudaGetLastError();
 }
 
