@@ -44,14 +44,14 @@ struct ose_batch {
     int2* d_work = nullptr;
     size_t work_cap = 0;
     std::vector<ose::BatchPass> passes;    // every pass of every application, in launch order
-    std::vector<int> pass_begin;           // passes of application n: [pass_begin[n], pass_begin[n + 1])
     char* arena = nullptr;
     size_t arena_bytes = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int it = 0;
-    int rows_scale = 2048, txy = 16, txz = 16, radix_order = 0;   // tunables
+    int rows_scale = 2048, txy = 16, txz = 16, radix_order = 0;   // tunables of the Stockham kernels
+    int group_mb = 0;      // shots per group: working set up to this many MB (0: one group)
     std::string err;
 };
 
@@ -98,64 +98,80 @@ void fill_descriptors(ose_batch* b)
     }
 }
 
-// Work lists of every application n: five passes (x forward, y forward,
-// z, y inverse, x inverse + update), each split by the axis length of the
-// shots: one launch per length the register kernels have (ose_cols.cu), one
-// launch of the Stockham kernels for all other lengths.
+// Work lists.  The shots are cut into groups whose working set (36 bytes per
+// cell: W, A, S, X, v) stays within group_mb MB, so that a group's fields can
+// stay in L2 through its whole step (0: all shots in one group).  For each
+// group, every application n runs five passes (x forward, y forward, z,
+// y inverse, x inverse + update), each split by the axis length of the
+// group's shots: one launch per length the register kernels have
+// (ose_cols.cu), one launch of the Stockham kernels for all other lengths.
 ose_status build_passes(ose_batch* b)
 {
     std::vector<int2> all;
-    struct Range { size_t off, count, smem; int kind, n_axis; };
+    struct Range { size_t off, count, smem; int kind, n_axis, n; };
     std::vector<Range> ranges;
-    std::vector<int> begin;
     b->passes.clear();
-    for (int n = 0; n <= b->Mmax; ++n) {
-        begin.push_back((int)ranges.size());
-        for (int kind = 0; kind < 5; ++kind) {
-            auto axis_len = [&](const ose::BatchShot& D) {
-                return kind == 0 || kind == 4 ? D.g.nxb : (kind == 2 ? D.g.nzb : D.g.nyb);
-            };
-            std::vector<int> lens;   // register classes present, then 0 = Stockham
-            for (int s = 0; s < b->nshots; ++s) {
-                const ose::BatchShot& D = b->desc[s];
-                if (D.M < n) continue;
-                const int L = ose::col_supported(axis_len(D)) ? axis_len(D) : 0;
-                if (std::find(lens.begin(), lens.end(), L) == lens.end()) lens.push_back(L);
-            }
-            std::sort(lens.begin(), lens.end(), [](int a, int c) { return a > c; });
-            for (int L : lens) {
-                const size_t off = all.size();
-                size_t sm = 0;
-                for (int s = 0; s < b->nshots; ++s) {
+    std::vector<std::vector<int>> groups(1);
+    double gbytes = 0.0;
+    for (int s = 0; s < b->nshots; ++s) {
+        const ose::Geometry& g = b->desc[s].g;
+        const double sb = 36.0 * (double)g.nxb * g.nyb * g.nzb;
+        if (b->group_mb > 0 && !groups.back().empty() && gbytes + sb > b->group_mb * 1048576.0) {
+            groups.emplace_back();
+            gbytes = 0.0;
+        }
+        groups.back().push_back(s);
+        gbytes += sb;
+    }
+    for (const std::vector<int>& grp : groups) {
+        int Mg = 0;
+        for (int s : grp) Mg = std::max(Mg, b->desc[s].M);
+        for (int n = 0; n <= Mg; ++n) {
+            for (int kind = 0; kind < 5; ++kind) {
+                auto axis_len = [&](const ose::BatchShot& D) {
+                    return kind == 0 || kind == 4 ? D.g.nxb : (kind == 2 ? D.g.nzb : D.g.nyb);
+                };
+                std::vector<int> lens;   // register classes present, 0 = Stockham
+                for (int s : grp) {
                     const ose::BatchShot& D = b->desc[s];
                     if (D.M < n) continue;
-                    const int len = axis_len(D);
-                    if ((ose::col_supported(len) ? len : 0) != L) continue;
-                    long long nb;
-                    if (L > 0) {
-                        if (kind == 0 || kind == 4)
-                            nb = ((long long)D.g.nyb * D.g.nzb + ose::row_tile(L) - 1) / ose::row_tile(L);
-                        else
-                            nb = (long long)((D.g.nxb + ose::col_tile(L) - 1) / ose::col_tile(L)) *
-                                 (kind == 2 ? D.g.nyb : D.g.nzb);
-                    } else if (kind == 0 || kind == 4) {
-                        nb = ((long long)D.g.nyb * D.g.nzb + D.rpc - 1) / D.rpc;
-                        sm = std::max(sm, ose::batch_rows_smem(D.g.nxb, D.rpc));
-                    } else if (kind == 2) {
-                        nb = (long long)(D.g.nxb + D.txz - 1) / D.txz * D.g.nyb;
-                        sm = std::max(sm, ose::batch_lines_smem(D.g.nzb, D.txz));
-                    } else {
-                        nb = (long long)(D.g.nxb + D.txy - 1) / D.txy * D.g.nzb;
-                        sm = std::max(sm, ose::batch_lines_smem(D.g.nyb, D.txy));
-                    }
-                    for (long long k = 0; k < nb; ++k) all.push_back(make_int2(s, (int)k));
+                    const int L = ose::col_supported(axis_len(D)) ? axis_len(D) : 0;
+                    if (std::find(lens.begin(), lens.end(), L) == lens.end()) lens.push_back(L);
                 }
-                if (sm > 227 * 1024) return bfail(b, OSE_ERR_UNSUPPORTED, "a tile does not fit shared memory");
-                ranges.push_back({off, all.size() - off, sm, kind, L});
+                std::sort(lens.begin(), lens.end(), [](int a, int c) { return a > c; });
+                for (int L : lens) {
+                    const size_t off = all.size();
+                    size_t sm = 0;
+                    for (int s : grp) {
+                        const ose::BatchShot& D = b->desc[s];
+                        if (D.M < n) continue;
+                        const int len = axis_len(D);
+                        if ((ose::col_supported(len) ? len : 0) != L) continue;
+                        long long nb;
+                        if (L > 0) {
+                            if (kind == 0 || kind == 4)
+                                nb = ((long long)D.g.nyb * D.g.nzb + ose::row_tile(L) - 1) / ose::row_tile(L);
+                            else
+                                nb = (long long)((D.g.nxb + ose::col_tile(L) - 1) / ose::col_tile(L)) *
+                                     (kind == 2 ? D.g.nyb : D.g.nzb);
+                        } else if (kind == 0 || kind == 4) {
+                            nb = ((long long)D.g.nyb * D.g.nzb + D.rpc - 1) / D.rpc;
+                            sm = std::max(sm, ose::batch_rows_smem(D.g.nxb, D.rpc));
+                        } else if (kind == 2) {
+                            nb = (long long)(D.g.nxb + D.txz - 1) / D.txz * D.g.nyb;
+                            sm = std::max(sm, ose::batch_lines_smem(D.g.nzb, D.txz));
+                        } else {
+                            nb = (long long)(D.g.nxb + D.txy - 1) / D.txy * D.g.nzb;
+                            sm = std::max(sm, ose::batch_lines_smem(D.g.nyb, D.txy));
+                        }
+                        for (long long k = 0; k < nb; ++k) all.push_back(make_int2(s, (int)k));
+                    }
+                    if (sm > 227 * 1024) return bfail(b, OSE_ERR_UNSUPPORTED, "a tile does not fit shared memory");
+                    ranges.push_back({off, all.size() - off, sm, kind, L, n});
+                }
             }
         }
     }
-    begin.push_back((int)ranges.size());
     if (all.size() > b->work_cap) {
         if (b->d_work) cudaFree(b->d_work);
         b->d_work = nullptr;
@@ -167,8 +183,7 @@ ose_status build_passes(ose_batch* b)
                            cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
     for (const Range& r : ranges)
-        b->passes.push_back({b->d_work + r.off, (int)r.count, r.smem, r.kind, r.n_axis});
-    b->pass_begin = begin;
+        b->passes.push_back({b->d_work + r.off, (int)r.count, r.smem, r.kind, r.n_axis, r.n});
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     return OSE_OK;
 }
@@ -177,14 +192,10 @@ cudaError_t enqueue_batch_step(ose_batch* b)
 {
     cudaError_t e = ose::launch_batch_inject(b->stream, b->d_shots, b->nshots);
     if (e != cudaSuccess) return e;
-    for (int n = 0; n <= b->Mmax; ++n) {
-        for (int i = b->pass_begin[n]; i < b->pass_begin[n + 1]; ++i) {
-            const ose::BatchPass& p = b->passes[i];
-            e = p.n_axis > 0 ? ose::launch_batch_col_pass(b->stream, p.kind, p.n_axis, b->d_shots, p.work,
-                                                          p.nblocks, n)
-                             : ose::launch_batch_stockham_pass(b->stream, b->d_shots, n, p);
-            if (e != cudaSuccess) return e;
-        }
+    for (const ose::BatchPass& p : b->passes) {
+        e = p.n_axis > 0 ? ose::launch_batch_col_pass(b->stream, p.kind, p.n_axis, b->d_shots, p.work, p.nblocks, p.n)
+                         : ose::launch_batch_stockham_pass(b->stream, b->d_shots, p.n, p);
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
@@ -512,9 +523,10 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
             char line[1 << 16];
             while (fgets(line, sizeof line, f)) {
                 char key[1 << 15];
-                int rs, ty, tz, ro;
-                if (sscanf(line, "%32767s %d %d %d %d", key, &rs, &ty, &tz, &ro) == 5 && sig == key) {
-                    b->rows_scale = rs; b->txy = ty; b->txz = tz; b->radix_order = ro;
+                int rs, ty, tz, ro, gm = 0;
+                const int nf = sscanf(line, "%32767s %d %d %d %d %d", key, &rs, &ty, &tz, &ro, &gm);
+                if (nf >= 5 && sig == key) {
+                    b->rows_scale = rs; b->txy = ty; b->txz = tz; b->radix_order = ro; b->group_mb = gm;
                     fclose(f);
                     fill_descriptors(b);
                     ose_status st = build_passes(b);
@@ -537,6 +549,14 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
     float best = 1e30f, ms = 0.f;
     ose_status st = measure(&best);
     if (st != OSE_OK) return st;
+    // group size first: it decides whether fields stay in L2 (1 MB: one shot
+    // per group, since every shot is larger)
+    for (int gm : {1024, 256, 96, 1}) {
+        const int keep = b->group_mb;
+        b->group_mb = gm;
+        if (measure(&ms) == OSE_OK && ms < best) best = ms;
+        else b->group_mb = keep;
+    }
     const int rs_c[] = {1024, 2048, 4096};
     const int tx_c[] = {8, 16, 32};
     for (int rs : rs_c) {
@@ -568,15 +588,17 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
     if (cache_path) {
         FILE* f = fopen(cache_path, "a");
         if (!f) return bfail(b, OSE_ERR_IO, std::string("cannot write ") + cache_path);
-        fprintf(f, "%s %d %d %d %d\n", sig.c_str(), b->rows_scale, b->txy, b->txz, b->radix_order);
+        fprintf(f, "%s %d %d %d %d %d\n", sig.c_str(), b->rows_scale, b->txy, b->txz, b->radix_order, b->group_mb);
         fclose(f);
     }
     return OSE_OK;
 }
 
-ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order)
+ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
+                                int* group_mb)
 {
     if (!b) return OSE_ERR_INVALID;
+    if (group_mb) *group_mb = b->group_mb;
     if (rows_scale) *rows_scale = b->rows_scale;
     if (txy) *txy = b->txy;
     if (txz) *txz = b->txz;

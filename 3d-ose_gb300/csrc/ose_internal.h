@@ -168,6 +168,7 @@ struct BatchPass {
     size_t smem;
     int kind;
     int n_axis;
+    int n;        // operator application
 };
 
 cudaError_t configure_batch_kernels();

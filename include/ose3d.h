@@ -360,12 +360,16 @@ ose_status ose_batch_info(const ose_batch* b, int shot, ose_derived* d, long lon
 ose_status ose_batch_get_gather(ose_batch* b, int shot, float* out);
 /* One shot's padded P or Q, [z][y][x]. */
 ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out);
-/* Pick the rows per x-pass block, the y/z column tile widths and the radix
- * order by timing candidates over `steps` steps (coordinate search); reuse a
- * cached choice for the same window sizes from cache_path (a text file, one
- * line per batch shape; NULL = no cache).  Resets the batch. */
+/* Pick the shot grouping (shots run in groups whose working set stays within
+ * group_mb MB, so a group's fields can stay in L2 through its step; 0 = all
+ * shots together) and, for axis lengths without register kernels, the rows
+ * per x-pass block, the y/z column tile widths and the radix order, by timing
+ * candidates over `steps` steps (coordinate search); reuse a cached choice for
+ * the same window sizes from cache_path (a text file, one line per batch
+ * shape; NULL = no cache).  Resets the batch. */
 ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, float* best_ms);
-ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order);
+ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
+                                int* group_mb);
 
 /* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
 #define OSE_NOALLOC_MAX_CELLS 262144
