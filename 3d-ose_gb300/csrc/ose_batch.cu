@@ -594,6 +594,20 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
     return OSE_OK;
 }
 
+ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb)
+{
+    if (!b || rows_scale < 1 || txy < 1 || txz < 1 || radix_order < 0 || radix_order > 1 || group_mb < 0)
+        return OSE_ERR_INVALID;
+    b->rows_scale = rows_scale;
+    b->txy = txy;
+    b->txz = txz;
+    b->radix_order = radix_order;
+    b->group_mb = group_mb;
+    fill_descriptors(b);
+    ose_status st = build_passes(b);
+    return st != OSE_OK ? st : ose_batch_reset(b);
+}
+
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
                                 int* group_mb)
 {

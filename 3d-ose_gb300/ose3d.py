@@ -44,7 +44,7 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_corrector_last_error", "ose_corrector_info", "ose_corrector_set_params",
            "ose_corrector_get_params", "ose_corrector_get_grads", "ose_corrector_forward",
            "ose_corrector_apply", "ose_corrector_train_sample", "ose_corrector_adam", "ose_corrector_loss",
-           "ose_rtm"]
+           "ose_rtm", "ose_batch_set_tuning"]
 CORRECTOR_SHELL = 16   # OSE_CORRECTOR_SHELL
 
 # void (*)(int it, const float* P, const float* Q, void* user)
@@ -168,6 +168,7 @@ def load_library(path: str = LIB_PATH):
         "ose_batch_get_gather": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_batch_get_wavefield": ([H, ctypes.c_int, ctypes.c_int, f32], ctypes.c_int),
         "ose_batch_autotune": ([H, ctypes.c_int, ctypes.c_char_p, f32], ctypes.c_int),
+        "ose_batch_set_tuning": ([H] + [ctypes.c_int] * 5, ctypes.c_int),
         "ose_batch_get_tuning": ([H, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)],
                                  ctypes.c_int),
         "ose_apply_operator_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
@@ -374,6 +375,9 @@ class Batch:
         self._check(self._lib.ose_batch_autotune(self._h, steps, cache_path.encode() if cache_path else None,
                                                  ctypes.byref(ms)))
         return ms.value
+
+    def set_tuning(self, rows_scale=2048, txy=16, txz=16, radix_order=0, group_mb=0):
+        self._check(self._lib.ose_batch_set_tuning(self._h, rows_scale, txy, txz, radix_order, group_mb))
 
     def tuning(self):
         v = [ctypes.c_int() for _ in range(5)]

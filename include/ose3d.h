@@ -370,6 +370,9 @@ ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out
 ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, float* best_ms);
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
                                 int* group_mb);
+/* Set the tuning by hand (the values ose_batch_get_tuning returns).  Resets
+ * the batch. */
+ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb);
 
 /* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
 #define OSE_NOALLOC_MAX_CELLS 262144
