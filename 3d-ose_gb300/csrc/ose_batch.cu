@@ -52,6 +52,13 @@ struct ose_batch {
     int it = 0;
     int rows_scale = 2048, txy = 16, txz = 16, radix_order = 0;   // tunables of the Stockham kernels
     int group_mb = 0;      // shots per group: working set up to this many MB (0: one group)
+    // lanes = 0: batched launches (one per pass and length class).  lanes = k
+    // > 0: every shot's own single-shot launches, shots spread round-robin
+    // over k streams that run concurrently inside the captured step.
+    int lanes = 0;
+    static constexpr int kMaxLanes = 8;
+    cudaStream_t lane[kMaxLanes] = {};
+    cudaEvent_t fork = nullptr, join[kMaxLanes] = {};
     std::string err;
 };
 
@@ -188,8 +195,77 @@ ose_status build_passes(ose_batch* b)
     return OSE_OK;
 }
 
+// One shot's whole step with the single-shot launch sequence (source
+// injection, then M + 1 applications of the generic passes) on stream st.
+cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
+{
+    const ose::BatchShot& D = b->desc[s];
+    cudaError_t e = ose::launch_inject(st, D.W, D.src, D.ricker, D.hil, D.ctr, D.nt);
+    if (e != cudaSuccess) return e;
+    ose::Tables t{};
+    t.twx = D.twx;
+    t.twy = D.twy;
+    t.twz = D.twz;
+    t.kx2 = D.kx2;
+    t.ky2 = D.ky2;
+    t.kz2 = D.kz2;
+    ose::EpiArgs ea{};
+    ea.vs = D.vs;
+    ea.ax = D.ax;
+    ea.ay = D.ay;
+    ea.az = D.az;
+    ea.S = D.S;
+    ea.wout = D.W;
+    ea.w = D.W;
+    ea.sch = D.sch;
+    ea.scl = D.scl;
+    ea.c0 = D.c0;
+    ea.c0l = D.c0l;
+    ea.gather = D.gather;
+    ea.cur = D.ctr + 1;
+    ea.gz = D.gz;
+    ea.bl = D.bl;
+    ea.bf = D.bf;
+    ea.nx = D.nx;
+    ea.ny = D.ny;
+    ea.nt = D.nt;
+    for (int n = 0; n <= D.M; ++n) {
+        const float2* an = n == 0 ? D.W : ((n & 1) ? D.A : D.W);
+        ea.prev = n == 0 ? D.A : ((n & 1) ? D.W : D.A);
+        ea.c1 = D.c[n];
+        ea.c1l = D.cl[n];
+        const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == D.M ? ose::EPI_LAST : ose::EPI_MID);
+        e = ose::launch_generic_application(st, D.g, D.px, D.py, D.pz, t, an, D.X, mode, ea, nullptr);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_lanes(ose_batch* b)
+{
+    cudaError_t e;
+    for (int k = 0; k < b->lanes; ++k) {
+        if (!b->lane[k] && (e = cudaStreamCreateWithFlags(&b->lane[k], cudaStreamNonBlocking)) != cudaSuccess)
+            return e;
+        if (!b->join[k] && (e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming)) != cudaSuccess)
+            return e;
+    }
+    if (!b->fork && (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(b->fork, b->stream)) != cudaSuccess) return e;
+    for (int k = 0; k < b->lanes; ++k)
+        if ((e = cudaStreamWaitEvent(b->lane[k], b->fork, 0)) != cudaSuccess) return e;
+    for (int s = 0; s < b->nshots; ++s)
+        if ((e = enqueue_shot_step(b, s, b->lane[s % b->lanes])) != cudaSuccess) return e;
+    for (int k = 0; k < b->lanes; ++k) {
+        if ((e = cudaEventRecord(b->join[k], b->lane[k])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(b->stream, b->join[k], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t enqueue_batch_step(ose_batch* b)
 {
+    if (b->lanes > 0) return enqueue_lanes(b);
     cudaError_t e = ose::launch_batch_inject(b->stream, b->d_shots, b->nshots);
     if (e != cudaSuccess) return e;
     for (const ose::BatchPass& p : b->passes) {
@@ -224,6 +300,11 @@ ose_status batch_graph(ose_batch* b)
 void free_batch(ose_batch* b)
 {
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (int k = 0; k < ose_batch::kMaxLanes; ++k) {
+        if (b->lane[k]) cudaStreamDestroy(b->lane[k]);
+        if (b->join[k]) cudaEventDestroy(b->join[k]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->d_work) cudaFree(b->d_work);
     if (b->d_shots) cudaFree(b->d_shots);
     if (b->arena) cudaFree(b->arena);
@@ -523,10 +604,12 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
             char line[1 << 16];
             while (fgets(line, sizeof line, f)) {
                 char key[1 << 15];
-                int rs, ty, tz, ro, gm = 0;
-                const int nf = sscanf(line, "%32767s %d %d %d %d %d", key, &rs, &ty, &tz, &ro, &gm);
+                int rs, ty, tz, ro, gm = 0, ln = 0;
+                const int nf = sscanf(line, "%32767s %d %d %d %d %d %d", key, &rs, &ty, &tz, &ro, &gm, &ln);
                 if (nf >= 5 && sig == key) {
                     b->rows_scale = rs; b->txy = ty; b->txz = tz; b->radix_order = ro; b->group_mb = gm;
+                    b->lanes = std::min(std::max(ln, 0), (int)ose_batch::kMaxLanes);
+                    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
                     fclose(f);
                     fill_descriptors(b);
                     ose_status st = build_passes(b);
@@ -549,9 +632,18 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
     float best = 1e30f, ms = 0.f;
     ose_status st = measure(&best);
     if (st != OSE_OK) return st;
-    // group size first: it decides whether fields stay in L2 (1 MB: one shot
-    // per group, since every shot is larger)
+    // batching strategy first: per-shot launches on 1, 2, 4 or 8 concurrent
+    // streams against batched launches (lanes = 0)
+    for (int ln : {1, 2, 4, 8}) {
+        const int keep = b->lanes;
+        b->lanes = ln;
+        if (measure(&ms) == OSE_OK && ms < best) best = ms;
+        else b->lanes = keep;
+    }
+    // then the group size of batched launches: it decides whether fields stay
+    // in L2 (1 MB: one shot per group, since every shot is larger)
     for (int gm : {1024, 256, 96, 1}) {
+        if (b->lanes > 0) break;
         const int keep = b->group_mb;
         b->group_mb = gm;
         if (measure(&ms) == OSE_OK && ms < best) best = ms;
@@ -588,16 +680,20 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
     if (cache_path) {
         FILE* f = fopen(cache_path, "a");
         if (!f) return bfail(b, OSE_ERR_IO, std::string("cannot write ") + cache_path);
-        fprintf(f, "%s %d %d %d %d %d\n", sig.c_str(), b->rows_scale, b->txy, b->txz, b->radix_order, b->group_mb);
+        fprintf(f, "%s %d %d %d %d %d %d\n", sig.c_str(), b->rows_scale, b->txy, b->txz, b->radix_order, b->group_mb,
+                b->lanes);
         fclose(f);
     }
     return OSE_OK;
 }
 
-ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb)
+ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb,
+                                int lanes)
 {
-    if (!b || rows_scale < 1 || txy < 1 || txz < 1 || radix_order < 0 || radix_order > 1 || group_mb < 0)
+    if (!b || rows_scale < 1 || txy < 1 || txz < 1 || radix_order < 0 || radix_order > 1 || group_mb < 0 ||
+        lanes < 0 || lanes > ose_batch::kMaxLanes)
         return OSE_ERR_INVALID;
+    b->lanes = lanes;
     b->rows_scale = rows_scale;
     b->txy = txy;
     b->txz = txz;
@@ -609,10 +705,11 @@ ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, 
 }
 
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
-                                int* group_mb)
+                                int* group_mb, int* lanes)
 {
     if (!b) return OSE_ERR_INVALID;
     if (group_mb) *group_mb = b->group_mb;
+    if (lanes) *lanes = b->lanes;
     if (rows_scale) *rows_scale = b->rows_scale;
     if (txy) *txy = b->txy;
     if (txz) *txz = b->txz;

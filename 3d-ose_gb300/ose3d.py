@@ -168,8 +168,8 @@ def load_library(path: str = LIB_PATH):
         "ose_batch_get_gather": ([H, ctypes.c_int, f32], ctypes.c_int),
         "ose_batch_get_wavefield": ([H, ctypes.c_int, ctypes.c_int, f32], ctypes.c_int),
         "ose_batch_autotune": ([H, ctypes.c_int, ctypes.c_char_p, f32], ctypes.c_int),
-        "ose_batch_set_tuning": ([H] + [ctypes.c_int] * 5, ctypes.c_int),
-        "ose_batch_get_tuning": ([H, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)],
+        "ose_batch_set_tuning": ([H] + [ctypes.c_int] * 6, ctypes.c_int),
+        "ose_batch_get_tuning": ([H] + [P(ctypes.c_int)] * 6,
                                  ctypes.c_int),
         "ose_apply_operator_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                         ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
@@ -376,13 +376,13 @@ class Batch:
                                                  ctypes.byref(ms)))
         return ms.value
 
-    def set_tuning(self, rows_scale=2048, txy=16, txz=16, radix_order=0, group_mb=0):
-        self._check(self._lib.ose_batch_set_tuning(self._h, rows_scale, txy, txz, radix_order, group_mb))
+    def set_tuning(self, rows_scale=2048, txy=16, txz=16, radix_order=0, group_mb=0, lanes=0):
+        self._check(self._lib.ose_batch_set_tuning(self._h, rows_scale, txy, txz, radix_order, group_mb, lanes))
 
     def tuning(self):
-        v = [ctypes.c_int() for _ in range(5)]
+        v = [ctypes.c_int() for _ in range(6)]
         self._check(self._lib.ose_batch_get_tuning(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("rows_scale", "txy", "txz", "radix_order", "group_mb"), (x.value for x in v)))
+        return dict(zip(("rows_scale", "txy", "txz", "radix_order", "group_mb", "lanes"), (x.value for x in v)))
 
 
 class Modeler:

@@ -360,19 +360,23 @@ ose_status ose_batch_info(const ose_batch* b, int shot, ose_derived* d, long lon
 ose_status ose_batch_get_gather(ose_batch* b, int shot, float* out);
 /* One shot's padded P or Q, [z][y][x]. */
 ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out);
-/* Pick the shot grouping (shots run in groups whose working set stays within
- * group_mb MB, so a group's fields can stay in L2 through its step; 0 = all
- * shots together) and, for axis lengths without register kernels, the rows
+/* Pick the batching strategy (lanes = 0: one batched launch per pass and axis
+ * length for all shots; lanes = k > 0: every shot's single-shot launches,
+ * shots spread over k streams that run concurrently in the captured step),
+ * the shot grouping of batched launches (groups whose working set stays
+ * within group_mb MB, so a group's fields can stay in L2 through its step;
+ * 0 = all shots together) and, for axis lengths without register kernels, the rows
  * per x-pass block, the y/z column tile widths and the radix order, by timing
  * candidates over `steps` steps (coordinate search); reuse a cached choice for
  * the same window sizes from cache_path (a text file, one line per batch
  * shape; NULL = no cache).  Resets the batch. */
 ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, float* best_ms);
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
-                                int* group_mb);
-/* Set the tuning by hand (the values ose_batch_get_tuning returns).  Resets
- * the batch. */
-ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb);
+                                int* group_mb, int* lanes);
+/* Set the tuning by hand (the values ose_batch_get_tuning returns; lanes <= 8).
+ * Resets the batch. */
+ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb,
+                                int lanes);
 
 /* Largest padded grid (nxb*nyb*nzb) ose_apply_operator_noalloc accepts. */
 #define OSE_NOALLOC_MAX_CELLS 262144

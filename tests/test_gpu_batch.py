@@ -79,3 +79,27 @@ def test_autotune_keeps_results_and_caches(tmp_path):
     with ose3d.Batch(p, m, WINDOWS) as b2:
         assert b2.autotune(steps=2, cache_path=cache) < 0    # served from the cache
         assert b2.tuning() == t1
+
+
+REG_WINDOWS = [dict(x0=0, y0=0, z0=0, nx=52, ny=52, nz=52, sx=20, sy=26, sz=3),     # padded 64^3 (register)
+               dict(x0=8, y0=4, z0=0, nx=84, ny=52, nz=36, sx=40, sy=20, sz=2),     # 96 x 64 x 48
+               dict(x0=20, y0=10, z0=2, nx=52, ny=84, nz=52, sx=30, sy=40, sz=5)]   # 64 x 96 x 64
+
+
+@pytest.mark.parametrize("lanes", [0, 3])
+def test_register_classes_and_lanes_match_single_shots(lanes):
+    """Windows whose padded axes have register kernels (64 = 16*4, 96 = 16*6),
+    batched launches (lanes 0) or per-shot launches on 3 concurrent streams:
+    bit for bit the single-shot handles."""
+    m = model(seed=9, shape=(100, 100, 60))
+    p = ose3d.default_params(**BASE)
+    with ose3d.Batch(p, m, REG_WINDOWS) as b:
+        b.set_tuning(lanes=lanes)
+        assert b.tuning()["lanes"] == lanes
+        b.run(BASE["nt"])
+        for s, w in enumerate(REG_WINDOWS):
+            with single(m, w) as h:
+                h.reset_shot(0)
+                g = h.run(BASE["nt"], want_gather=True)
+                assert np.array_equal(b.gather(s), g)
+                assert np.array_equal(b.wavefield(s, ose3d.FIELD_Q), h.wavefield(ose3d.FIELD_Q))
