@@ -711,8 +711,11 @@ ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
     for (int i = 0; i < 6; ++i)
         if (shell < 1 || sp[i] > shell) return fail(h, OSE_ERR_INVALID, "the shell must be at least as wide as every sponge");
     ose::learn::NetGeom g{h->d.nxb, h->d.nyb, h->d.nzb, shell, {sp[0], sp[1], sp[2], sp[3], sp[4], sp[5]}};
+    // the tensor-core kernels unless OSE3D_CORRECTOR=fp32 asks for the FP32 ones
+    const char* mode = getenv("OSE3D_CORRECTOR");
+    const bool fp32 = mode && strcmp(mode, "fp32") == 0;
     h->corr = ose::learn::new_corrector();
-    cudaError_t e = ose::learn::create_net(h->corr, g, false);
+    cudaError_t e = ose::learn::create_net(h->corr, g, false, fp32);
     if (e == cudaSuccess)
         e = cudaMemcpy(ose::learn::net_of(h->corr).params, params, sizeof(float) * ose::learn::param_count(),
                        cudaMemcpyHostToDevice);
@@ -725,9 +728,7 @@ ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
         e = cudaMalloc((void**)&h->tcerr, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(h->tcerr, 0, sizeof(int));
     }
-    // the tensor-core kernels unless OSE3D_CORRECTOR=fp32 asks for the FP32 ones
-    const char* mode = getenv("OSE3D_CORRECTOR");
-    if (e == cudaSuccess && !(mode && strcmp(mode, "fp32") == 0)) e = ose::learn::create_tc(h->corr, params, h->tcerr);
+    if (e == cudaSuccess && !fp32) e = ose::learn::create_tc(h->corr, params, h->tcerr);
     if (e != cudaSuccess) {
         ose::learn::delete_corrector(h->corr);
         h->corr = nullptr;

@@ -639,7 +639,7 @@ namespace learn {
 
 // Allocates a network for a grid; training = also gradients, Adam moments
 // and backward buffers.
-cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training)
+cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training, bool fp32_forward)
 {
     Net& n = c->net;
     n.g = g;
@@ -658,8 +658,10 @@ cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training)
     A_(n.loss, 1);
     A_(n.sloc, cells);
     A_(n.stmp, cells);
-    A_(n.F, cells * 8);
-    for (int l = 0; l < 3; ++l) A_(n.A[l], cells * 32);
+    if (training || fp32_forward) {   // the tensor-core forward keeps its own BF16 activations
+        A_(n.F, cells * 8);
+        for (int l = 0; l < 3; ++l) A_(n.A[l], cells * 32);
+    }
     if (training) {
         A_(n.grads, np);
         A_(n.m, np);
@@ -733,7 +735,7 @@ ose_status ose_corrector_create(int nxb, int nyb, int nzb, int shell, const int*
         if (sponge[i] < 0 || sponge[i] > shell) return corr_fail(nullptr, OSE_ERR_INVALID, "sponge widths must be 0..shell");
     ose_corrector* c = new ose_corrector();
     ose::learn::NetGeom g{nxb, nyb, nzb, shell, {sponge[0], sponge[1], sponge[2], sponge[3], sponge[4], sponge[5]}};
-    cudaError_t e = ose::learn::create_net(c, g, true);
+    cudaError_t e = ose::learn::create_net(c, g, true, true);
     if (e != cudaSuccess) {
         ose_status s = corr_fail(nullptr, e == cudaErrorMemoryAllocation ? OSE_ERR_NOMEM : OSE_ERR_CUDA,
                                  std::string("corrector allocation: ") + cudaGetErrorString(e));

@@ -82,7 +82,7 @@ cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W,
 // Corrector objects (the C ABI's ose_corrector) for the modeler's own use.
 ose_corrector* new_corrector();
 void delete_corrector(ose_corrector* c);
-cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training);
+cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training, bool fp32_forward);
 const Net& net_of(const ose_corrector* c);
 // Tensor-core buffers for inference from FP32 host parameters; err = the
 // device error word the kernels report to.

@@ -133,13 +133,13 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
+def ncu_traffic(workload: str, kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        return t.get(WORKLOAD, {}).get(kernel)
+        return t.get(workload, {}).get(kernel)
     except Exception:
         return None
 
@@ -306,7 +306,7 @@ def run_learned(args, rank):
     n = 240
     vel = workloads.smooth_random_salt(n, n, n, seed=505)
     K = max(1, min(args.steps, 100))
-    acc_steps = 300
+    acc_steps = 0 if args.no_accuracy else 300
     kw = lambda sp: LB.pair_params(n, 20.0, (120, 120, 8), acc_steps + K + 10, sp)  # noqa: E731
     res = {}
     wide_int = []
@@ -331,7 +331,7 @@ def run_learned(args, rank):
                 w = wide_int[t // every]
                 err += float(((buf - w) ** 2).sum())
                 ref += float((w ** 2).sum())
-        g = np.concatenate(rows)
+        g = np.concatenate(rows) if rows else np.zeros((0, 1), np.float32)
         m.run(max(3, args.warmup))
         ms = m.run_timed(K)
         prof, _ = m.profile_step(reps=1)
@@ -342,7 +342,7 @@ def run_learned(args, rank):
         if mode == "wide":
             ref_rows = g
             wide_cells = cells
-        else:
+        elif acc_steps:
             r["interior_error_energy"] = err / max(ref, 1e-300)
             r["gather_rel_l2"] = float(np.linalg.norm(g - ref_rows) / np.linalg.norm(ref_rows))
         res[mode] = r
@@ -368,7 +368,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched64", "precision", "learned"])
+    ap.add_argument("--no-accuracy", action="store_true", help="learned workload: timing only")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=[WORKLOAD, "ose320x288x256", "ose384x384x256", "ose142", "batched64", "precision",
+                             "learned"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -390,7 +393,8 @@ def main():
     import ose3d
     import workloads
 
-    build, kw = workloads.CONFIGS[WORKLOAD]
+    wl = args.workload
+    build, kw = workloads.CONFIGS[wl]
     vel = build()
     warm = max(3, args.warmup)
     if warm + args.steps + 1 > kw["nt"]:
@@ -423,7 +427,7 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": ncu_traffic(dom["name"]),
+                "traffic": ncu_traffic(wl, dom["name"]),
                 "algorithmic_bytes_per_launch": dom["bytes"], "ms_per_launch": dom["ms"],
                 "kernel_shares": {k: v / total for k, v in share.items()},
                 "step_bytes_model": sum(r["bytes"] * per_step[r["name"]] for r in rows) / cells,
@@ -454,16 +458,16 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, t = oracle_rate(kw, vel, 1)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"1 full-size {WORKLOAD} step on the FP64 CPU oracle ({t:.1f} s)"}
+               "sample": f"1 full-size {wl} step on the FP64 CPU oracle ({t:.1f} s)"}
     dist.close()
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": DATA,
-            "config": {"workload": WORKLOAD, "text": WORKLOAD_TEXT, "grid": [d.nxb, d.nyb, d.nzb],
+            "config": {"workload": wl, "text": WORKLOAD_TEXT if wl == WORKLOAD else wl, "grid": [d.nxb, d.nyb, d.nzb],
                        "M": d.M, "kernel_path": "generic" if d.path == 0 else "plane",
-                       "l2": "inputs larger than L2 (each field 134 MB; 0.6 GB resident)",
+                       "l2": f"inputs larger than L2 (each field {cells * 8 / 1e6:.0f} MB)",
                        "parallelism": f"replicas x{world} (one independent shot per GPU)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps, "clocks": clocks}
