@@ -141,6 +141,8 @@ struct ColCfg {
     static constexpr int TX = P > 16 ? 8 : 16;     // columns per CTA
     static constexpr int THREADS = TX * P;
     static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)N * TX);
+    // CTAs per SM asked of the register allocator: about 80 registers a thread
+    static constexpr int MINB = C == 23 ? 1 : 65536 / (THREADS * 80);
 };
 
 // Lines at base + n * stride of the columns x0 .. x0 + TX - 1 (x tile xt);
@@ -219,7 +221,7 @@ __device__ __forceinline__ void col_body(float2* __restrict__ X, int nxb, long l
 }
 
 template <int C, int MODE>
-__global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__ X, int nxb, long long stride,
+__global__ void __launch_bounds__(ColCfg<C>::THREADS, ColCfg<C>::MINB) k_col(float2* __restrict__ X, int nxb, long long stride,
                                                             long long ostride, const float2* __restrict__ twg,
                                                             Tables tb)
 {
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(ColCfg<C>::THREADS) k_col(float2* __restrict__
 // Batched: CTA b works on block work[b].y = x tile + (x tiles) * other of
 // shot work[b].x; AXIS 1 = y lines, 2 = z lines.
 template <int C, int MODE, int AXIS>
-__global__ void __launch_bounds__(ColCfg<C>::THREADS) kb_col(const BatchShot* __restrict__ shots,
+__global__ void __launch_bounds__(ColCfg<C>::THREADS, ColCfg<C>::MINB) kb_col(const BatchShot* __restrict__ shots,
                                                              const int2* __restrict__ work)
 {
     extern __shared__ float4 smem4[];
@@ -314,11 +316,7 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
             for (int k1 = 0; k1 < 16; ++k1) v[k1] = Tr[q * 17 + k1];
             dftc<16, C, true>(v, W);
             const int y = (int)(row % nyb), z = (int)(row / nyb);
-#pragma unroll
-            for (int n1 = 0; n1 < 16; ++n1) {
-                const int x = C * n1 + q;
-                epilogue<EPI>(row * N + x, x, y, z, v[n1], e);
-            }
+            epilogue_row<EPI, 16>(v, row * N + q, q, C, y, z, e);
         }
     }
 }

@@ -63,6 +63,84 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
     }
 }
 
+// The same work for cnt cells of one row held by one thread, x = x0 + k * xs,
+// i = i0 + k * xs: every load of a chunk of 8 cells is issued before the
+// first store, so the loads overlap (the per-cell arithmetic is epilogue's).
+template <int EPI, int CNT>
+__device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int x0, int xs, int y, int z,
+                                             const EpiArgs& e)
+{
+    constexpr int CH = 8;
+    static_assert(CNT % CH == 0, "whole chunks");
+#pragma unroll
+    for (int h = 0; h < CNT / CH; ++h) {
+        float vv[CH], axv[CH];
+        float2 am[CH], sm[CH];
+#pragma unroll
+        for (int q = 0; q < CH; ++q) {
+            const int k = CH * h + q;
+            const long long i = i0 + (long long)k * xs;
+            vv[q] = __ldg(e.vs + i);
+            if (EPI == EPI_FIRST) am[q] = e.w[i];
+            if (EPI == EPI_MID || EPI == EPI_LAST) {
+                am[q] = e.prev[i];
+                sm[q] = e.S[i];
+                axv[q] = __ldg(e.ax + x0 + k * xs);
+            }
+        }
+        float ayz0 = 0.f, ayz1 = 0.f;
+        if (EPI == EPI_MID || EPI == EPI_LAST) {
+            ayz0 = __ldg(e.ay + y);
+            ayz1 = __ldg(e.az + z);
+        }
+#pragma unroll
+        for (int q = 0; q < CH; ++q) {
+            const int k = CH * h + q;
+            const long long i = i0 + (long long)k * xs;
+            const int x = x0 + k * xs;
+            const float2 X = v[k];
+            float2 Lx = make_float2(X.x * vv[q], X.y * vv[q]);
+            if (kCompensatedConstants || EPI == EPI_SCALE_VEL)
+                Lx = make_float2(fmaf(Lx.x, e.sch, Lx.x * e.scl), fmaf(Lx.y, e.sch, Lx.y * e.scl));
+            if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
+                e.prev[i] = Lx;
+            } else if (EPI == EPI_FIRST) {
+                const float2 a1 = make_float2(Lx.y, -Lx.x);
+                const float2 w = am[q];
+                e.prev[i] = a1;
+                if (kCompensatedConstants)
+                    e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
+                                         fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
+                else
+                    e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+            } else {
+                const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
+                const float att = axv[q] * ayz0 * ayz1;
+                float2 s = sm[q];
+                if (kCompensatedConstants) {
+                    s.x = fmaf(e.c1l, an.x, s.x);
+                    s.y = fmaf(e.c1l, an.y, s.y);
+                }
+                s.x = fmaf(e.c1, an.x, s.x) * att;
+                s.y = fmaf(e.c1, an.y, s.y) * att;
+                if (EPI == EPI_MID) {
+                    e.prev[i] = an;
+                    e.S[i] = s;
+                } else {
+                    e.wout[i] = s;
+                    if (z == e.gz) {
+                        const int ix = x - e.bl, iy = y - e.bf;
+                        if (ix >= 0 && ix < e.nx && iy >= 0 && iy < e.ny) {
+                            const int c = *e.cur;
+                            if (c >= 0 && c < e.nt) e.gather[(long long)c * e.nx * e.ny + iy * e.nx + ix] = s.y;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
 // The epilogue arguments of batched shot S at application n.
 __device__ __forceinline__ EpiArgs batch_epi(const BatchShot& S, int n)
 {
