@@ -2,11 +2,10 @@
 // cores: each 3x3x3 convolution layer is an implicit GEMM with BF16 weights
 // and activations and an FP32 accumulator in TMEM.
 //
-// Output tiles are 8 (x) x 16 (y) x 1 (z) = 128 cells, the M rows of the MMA
-// (row m = y * 8 + x); one persistent CTA per SM takes four tiles at a time
-// with four TMEM accumulators.  A tile's input halo, 10 x 18 x 3 cells with
-// all input channels, sits once in shared memory in the layout [z 3][y 18]
-// [channel chunk][x 10][8 channels x 2 bytes]: for a tap
+// A CTA computes output tiles of 8 (x) x 16 (y) x 1 (z) = 128 cells, the M
+// rows of the MMA (row m = y * 8 + x).  It stages the input halo of the tile,
+// 10 x 18 x 3 cells with all input channels, once in shared memory in the
+// layout [z 3][y 18][channel chunk][x 10][8 channels x 2 bytes]: for a tap
 // (dx, dy, dz) the 128 x Cin operand is then a plain K-major descriptor into
 // the halo (rows 16 bytes apart, y groups SBO apart, channel chunks LBO apart,
 // start shifted by dx * 16 bytes), so no im2col copy is made.  A tile is
@@ -36,7 +35,7 @@ namespace {
 
 constexpr int TXW = 8, TYW = 16;              // output tile (x, y), one z plane
 constexpr int HX = TXW + 2, HY = TYW + 2, HZ = 3;
-constexpr int THREADS = 256;                  // 8 warps: 2 per TMEM lane quarter
+constexpr int THREADS = 128;                  // one output row (cell) per thread
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -69,8 +68,6 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     return u;
 }
 
-constexpr int G = 4;   // tiles per CTA iteration: four independent accumulators
-
 template <int CIN, int NPAD>
 struct LayerCfg {
     static constexpr int chunks = CIN / 8;                       // 16-byte channel chunks
@@ -81,97 +78,24 @@ struct LayerCfg {
     static constexpr int w_bytes = 27 * ngroups * chunks * 128;  // B operands, all taps
     static constexpr uint32_t wsbo = chunks * 128;               // B: n-group stride
     static constexpr int ksteps = CIN / 16;
-    static constexpr int off_w = G * halo_bytes;                 // G halo buffers first
+    static constexpr int off_w = halo_bytes;
     static constexpr int off_bias = off_w + w_bytes;
     static constexpr int off_bar = off_bias + NPAD * 4;
     static constexpr int smem = off_bar + 16;
     static constexpr uint32_t id = tc5::idesc(tc5::kTypeBF16, 128, NPAD);
-    static constexpr int UNITS = HZ * HY * HX * chunks;          // 16-byte halo units
-    static constexpr int PER = (UNITS + THREADS - 1) / THREADS;
 };
-
-// One tile's input halo into H: every load of the thread is issued before the
-// first shared-memory store.  MODE 0 builds the features from the state and
-// the velocity; otherwise the BF16 activations are copied.
-template <int CIN, int NPAD, int MODE>
-__device__ __forceinline__ void load_halo(uint8_t* H, int tp, const uint16_t* __restrict__ act_in,
-                                          const float2* __restrict__ Win, const float* __restrict__ vel,
-                                          const float* __restrict__ sloc, const NetGeom& g)
-{
-    using C = LayerCfg<CIN, NPAD>;
-    const int t = threadIdx.x;
-    const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
-    if (MODE == 0) {
-        float2 wv[C::PER];
-        float vv[C::PER], sv[C::PER];
-        bool ok[C::PER];
-#pragma unroll
-        for (int k = 0; k < C::PER; ++k) {
-            const int u = t + k * THREADS;
-            const int ch = u % C::chunks, cell = u / C::chunks;
-            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-            const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-            ok[k] = u < C::UNITS && ch == 0 && in_shell(g, x, y, z);
-            const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-            wv[k] = ok[k] ? __ldg(Win + c) : make_float2(0.f, 0.f);
-            vv[k] = ok[k] ? __ldg(vel + c) : 0.f;
-            sv[k] = ok[k] ? __ldg(sloc + c) : 1.f;
-        }
-#pragma unroll
-        for (int k = 0; k < C::PER; ++k) {
-            const int u = t + k * THREADS;
-            if (u >= C::UNITS) break;
-            const int ch = u % C::chunks, cell = u / C::chunks;
-            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (ok[k]) {
-                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-                const float inv = 1.f / sv[k];
-                v.x = pack2(wv[k].x * inv, wv[k].y * inv);
-                v.y = pack2(vv[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
-                v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
-            }
-            *reinterpret_cast<uint4*>(H + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
-        }
-    } else {
-        uint4 v[C::PER];
-#pragma unroll
-        for (int k = 0; k < C::PER; ++k) {
-            const int u = t + k * THREADS;
-            const int ch = u % C::chunks, cell = u / C::chunks;
-            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-            const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-            const bool ok = u < C::UNITS && in_shell(g, x, y, z);
-            const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-            v[k] = ok ? __ldg(reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8)) : make_uint4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int k = 0; k < C::PER; ++k) {
-            const int u = t + k * THREADS;
-            if (u >= C::UNITS) break;
-            const int ch = u % C::chunks, cell = u / C::chunks;
-            const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-            *reinterpret_cast<uint4*>(H + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v[k];
-        }
-    }
-}
 
 // MODE 0: layer 0 (features from state + velocity), hidden output (ReLU, BF16)
 // MODE 1: hidden layer, BF16 in, hidden output
 // MODE 2: output layer, BF16 in, state += s(x) (o0, o1) at the write cells
-// (sloc = the local scale s(x) per cell).
-// A CTA takes G consecutive tiles per iteration, one accumulator (32 TMEM
-// columns) and one halo buffer each, and issues their MMAs interleaved tap by
-// tap, so G independent accumulation chains share the tensor pipe.  Warps w
-// and w + 4 read TMEM lanes 32 (w % 4) .. + 31: warps 0-3 the first G/2
-// tiles, warps 4-7 the others.
+// (scal = the local scale s(x) per cell)
 template <int CIN, int NPAD, int MODE>
-__global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const uint16_t* __restrict__ act_in,
-                                                        const float2* __restrict__ Win, const float* __restrict__ vel,
-                                                        const uint8_t* __restrict__ wts, const float* __restrict__ bias,
-                                                        uint16_t* __restrict__ act_out, float2* __restrict__ state,
-                                                        const float* __restrict__ sloc, NetGeom g,
-                                                        const int* __restrict__ tiles, int ntiles, int* err)
+__global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict__ act_in,
+                                                     const float2* __restrict__ Win, const float* __restrict__ vel,
+                                                     const uint8_t* __restrict__ wts, const float* __restrict__ bias,
+                                                     uint16_t* __restrict__ act_out, float2* __restrict__ state,
+                                                     const float* __restrict__ scal, NetGeom g,
+                                                     const int* __restrict__ tiles, int ntiles, int* err)
 {
     using C = LayerCfg<CIN, NPAD>;
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -179,9 +103,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const uint16_t* __restri
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::off_bar + 8);
     float* sb = reinterpret_cast<float*>(sm + C::off_bias);
     const uint32_t sbase = tc5::smem_u32(sm);
-    const int t = threadIdx.x, warp = t >> 5, quarter = warp & 3, half = warp >> 2;
+    const int t = threadIdx.x, warp = t >> 5;
 
-    if (warp == 0) tc5::tmem_alloc(tslot, 32 * G);
+    if (warp == 0) tc5::tmem_alloc(tslot, 32);
     if (t == 0) tc5::mbar_init(bar, 1);
     {
         const int4* s4 = reinterpret_cast<const int4*>(wts);
@@ -193,34 +117,87 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const uint16_t* __restri
     __syncthreads();
     tc5::fence_after_sync();
     const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     int failed = 0;
     uint32_t phase = 0;
-    const int ngroups_all = (ntiles + G - 1) / G;
 
-    for (int grp = blockIdx.x; grp < ngroups_all; grp += gridDim.x) {
-        const int t0 = grp * G;
-        const int nt = min(G, ntiles - t0);
-        for (int h = 0; h < nt; ++h)
-            load_halo<CIN, NPAD, MODE>(sm + h * C::halo_bytes, tiles[t0 + h], act_in, Win, vel, sloc, g);
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const int tp = tiles[tile];
+        const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
+        // halo: HZ * HY * HX cells x chunks 16-byte units; every load of the
+        // thread is issued before the first store so they overlap
+        constexpr int UNITS = HZ * HY * HX * C::chunks;
+        constexpr int PER = (UNITS + THREADS - 1) / THREADS;
+        if (MODE == 0) {
+            float2 wv[PER];
+            float vv[PER], sv[PER];
+            bool ok[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                ok[k] = u < UNITS && ch == 0 && in_shell(g, x, y, z);
+                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+                wv[k] = ok[k] ? __ldg(Win + c) : make_float2(0.f, 0.f);
+                vv[k] = ok[k] ? __ldg(vel + c) : 0.f;
+                sv[k] = ok[k] ? __ldg(scal + c) : 1.f;
+            }
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                if (u >= UNITS) break;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (ok[k]) {
+                    const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                    const float inv = 1.f / sv[k];
+                    v.x = pack2(wv[k].x * inv, wv[k].y * inv);
+                    v.y = pack2(vv[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
+                    v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
+                }
+                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
+            }
+        } else {
+            uint4 v[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
+                const bool ok = u < UNITS && in_shell(g, x, y, z);
+                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+                v[k] = ok ? __ldg(reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8)) : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int u = t + k * THREADS;
+                if (u >= UNITS) break;
+                const int ch = u % C::chunks, cell = u / C::chunks;
+                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
+                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v[k];
+            }
+        }
         tc5::fence_async_smem();
         tc5::fence_before_sync();
         __syncthreads();
         int bad = 0;
         if (t == 0) {
             tc5::fence_after_sync();
+            uint32_t acc = 0;
             for (int tap = 0; tap < 27; ++tap) {
                 const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-                const uint32_t aoff = ((1 + dz) * HY + (1 + dy)) * C::sbo + (1 + dx) * 16;
+                const uint32_t a0 = sbase + ((1 + dz) * HY + (1 + dy)) * C::sbo + (1 + dx) * 16;
                 const uint32_t b0 = sbase + C::off_w + tap * C::ngroups * C::chunks * 128;
 #pragma unroll
                 for (int k = 0; k < C::ksteps; ++k) {
+                    const uint64_t da = tc5::smem_desc(a0 + 2 * k * C::lbo, C::lbo, C::sbo);
                     const uint64_t db = tc5::smem_desc(b0 + 2 * k * 128, 128, C::wsbo);
-                    const uint32_t acc = (tap | k) ? 1u : 0u;
-                    for (int h = 0; h < nt; ++h) {
-                        const uint32_t a0 = sbase + h * C::halo_bytes + aoff;
-                        const uint64_t da = tc5::smem_desc(a0 + 2 * k * C::lbo, C::lbo, C::sbo);
-                        tc5::mma_f16(tmem + 32 * h, da, db, C::id, acc);
-                    }
+                    tc5::mma_f16(tmem, da, db, C::id, acc);
+                    acc = 1;
                 }
             }
             tc5::mma_commit(bar);
@@ -230,40 +207,32 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const uint16_t* __restri
         phase ^= 1u;
         if (failed) break;
         tc5::fence_after_sync();
-        const int m = quarter * 32 + (t & 31);
+        const int x = x0 + (t & 7), y = y0 + (t >> 3), z = z0;
+        const bool valid = x < g.nx && y < g.ny && in_shell(g, x, y, z);
+        const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+        if (MODE == 2) {
+            float o[16];
+            tc5::tmem_ld16(trow, o);
+            if (valid && is_write(g, x, y, z)) {
+                const float sc = scal[c];
+                float2 w = state[c];
+                w.x = fmaf(sc, o[0] + sb[0], w.x);
+                w.y = fmaf(sc, o[1] + sb[1], w.y);
+                state[c] = w;
+            }
+        } else {
+            float o[32];
+            tc5::tmem_ld32(trow, o);
+            if (valid) {
+                uint4* dst = reinterpret_cast<uint4*>(act_out + c * 32);
 #pragma unroll
-        for (int hh = 0; hh < G / 2; ++hh) {
-            const int h = half * (G / 2) + hh;
-            const int tp = h < nt ? tiles[t0 + h] : 0;
-            const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
-            const int x = x0 + (m & 7), y = y0 + (m >> 3), z = z0;
-            const bool valid = h < nt && x < g.nx && y < g.ny && in_shell(g, x, y, z);
-            const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(32 * h);
-            if (MODE == 2) {
-                float o[16];
-                tc5::tmem_ld16(trow, o);
-                if (valid && is_write(g, x, y, z)) {
-                    const float sc = sloc[c];
-                    float2 w = state[c];
-                    w.x = fmaf(sc, o[0] + sb[0], w.x);
-                    w.y = fmaf(sc, o[1] + sb[1], w.y);
-                    state[c] = w;
-                }
-            } else {
-                float o[32];
-                tc5::tmem_ld32(trow, o);
-                if (valid) {
-                    uint4* dst = reinterpret_cast<uint4*>(act_out + c * 32);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const float* r = o + 8 * q;
-                        const float* b = sb + 8 * q;
-                        dst[q] = make_uint4(pack2(fmaxf(r[0] + b[0], 0.f), fmaxf(r[1] + b[1], 0.f)),
-                                            pack2(fmaxf(r[2] + b[2], 0.f), fmaxf(r[3] + b[3], 0.f)),
-                                            pack2(fmaxf(r[4] + b[4], 0.f), fmaxf(r[5] + b[5], 0.f)),
-                                            pack2(fmaxf(r[6] + b[6], 0.f), fmaxf(r[7] + b[7], 0.f)));
-                    }
+                for (int q = 0; q < 4; ++q) {
+                    const float* r = o + 8 * q;
+                    const float* b = sb + 8 * q;
+                    dst[q] = make_uint4(pack2(fmaxf(r[0] + b[0], 0.f), fmaxf(r[1] + b[1], 0.f)),
+                                        pack2(fmaxf(r[2] + b[2], 0.f), fmaxf(r[3] + b[3], 0.f)),
+                                        pack2(fmaxf(r[4] + b[4], 0.f), fmaxf(r[5] + b[5], 0.f)),
+                                        pack2(fmaxf(r[6] + b[6], 0.f), fmaxf(r[7] + b[7], 0.f)));
                 }
             }
         }
@@ -278,7 +247,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const uint16_t* __restri
     __syncthreads();
     if (warp == 0) {
         tc5::fence_after_sync();
-        tc5::tmem_dealloc(tmem, 32 * G);
+        tc5::tmem_dealloc(tmem, 32);
     }
 }
 
@@ -348,7 +317,7 @@ cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W,
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    const unsigned grid = (unsigned)std::max(1, std::min((tc.ntiles + G - 1) / G, sms));
+    const unsigned grid = (unsigned)std::max(1, std::min(tc.ntiles, 2 * sms));
     cudaError_t e = shell_scale(s, n, W);
     if (e != cudaSuccess) return e;
     k_conv_tc<16, 32, 0><<<grid, THREADS, LayerCfg<16, 32>::smem, s>>>(
