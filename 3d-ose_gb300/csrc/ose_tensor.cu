@@ -135,8 +135,13 @@ __device__ __forceinline__ float2 cmulf_conj(float2 a, float2 w)
 }
 
 // grid (nxb / TX, nyb); X is [z][y][x] with nzb = 256, transformed in place.
+// CTAs per SM asked of the register allocator (85 registers a thread for
+// three; shared memory allows three for TF32 and BF16X3, two for TF32X3)
 template <int VAR>
-__global__ void __launch_bounds__(THREADS) k_ztc(float2* __restrict__ X, int nxb, int nyb,
+constexpr int ztc_min_blocks() { return Cfg<VAR>::smem * 3 <= 227 * 1024 ? 3 : 2; }
+
+template <int VAR>
+__global__ void __launch_bounds__(THREADS, ztc_min_blocks<VAR>()) k_ztc(float2* __restrict__ X, int nxb, int nyb,
                                                  const uint8_t* __restrict__ bmat, Tables t, int* err)
 {
     using C = Cfg<VAR>;
