@@ -44,6 +44,10 @@ struct ose_handle {
     float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
     float *ricker = nullptr, *hil = nullptr;
     float* gather = nullptr; // [nt][ng]
+    // receiver list (ose_set_receivers): padded-grid cell index per receiver
+    // on the device, interior (x, y, z) on the host; empty = the receiver plane
+    long long* rec_idx = nullptr;
+    std::vector<int> rec_xyz;
     int* ctr = nullptr;      // [0] next step, [1] current step
     size_t bytes = 0;
     // precision form: mode, DFT operands of the tensor-core z pass, error word
@@ -117,7 +121,7 @@ void free_all(ose_handle* h)
     if (h->graph) cudaGraphExecDestroy(h->graph);
     void* bufs[] = {h->W, h->A, h->S, h->X, h->vs, h->ax, h->ay, h->az, h->kx2, h->ky2, h->kz2,
                     h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr,
-                    h->kx2l, h->ky2l, h->kz2l, h->twxl, h->tcb, h->tcerr};
+                    h->kx2l, h->ky2l, h->kz2l, h->twxl, h->tcb, h->tcerr, h->rec_idx};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -153,6 +157,26 @@ cudaError_t timed(ose::KernelTiming* tm, cudaStream_t s, int cls, double bytes, 
         tm->bytes[cls] += bytes;
     }
     return e;
+}
+
+// Receiver list: Q of step ctr[1] at the listed cells (rec_shotdata_3d's
+// gxyz form, ose_3d_kernel.cu:412-421).
+__global__ void k_record_list(const float2* __restrict__ W, const long long* __restrict__ idx, int n,
+                              float* __restrict__ gather, const int* __restrict__ ctr, int nt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = ctr[1];
+    if (i < n && c >= 0 && c < nt) gather[(size_t)c * n + i] = W[idx[i]].y;
+}
+
+cudaError_t enqueue_receivers(ose_handle* h, ose::KernelTiming* tm)
+{
+    if (h->rec_xyz.empty()) return cudaSuccess;
+    const int n = h->d.ng;
+    return timed(tm, h->stream, 5, 12.0 * n, [&] {
+        k_record_list<<<(n + 255) / 256, 256, 0, h->stream>>>(h->W, h->rec_idx, n, h->gather, h->ctr, h->p.nt);
+        return cudaGetLastError();
+    });
 }
 
 // The learned boundary correction at the end of a step (timing class 6;
@@ -195,7 +219,7 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm, bool source
     ea.wout = h->W;
     ea.gather = h->gather;
     ea.cur = h->ctr + 1;
-    ea.gz = h->p.bu + h->p.gzbeg;
+    ea.gz = h->rec_xyz.empty() ? h->p.bu + h->p.gzbeg : -1;   // a receiver list records separately
     ea.bl = h->p.bl;
     ea.bf = h->p.bf;
     ea.nx = h->p.nx;
@@ -228,6 +252,7 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm, bool source
         e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->tables, ea); });
         if (e != cudaSuccess) return e;
     }
+    if (source && (e = enqueue_receivers(h, tm)) != cudaSuccess) return e;
     return enqueue_corrector(h, tm);
 }
 
@@ -252,7 +277,7 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = tru
     ea.wout = h->W;
     ea.gather = h->gather;
     ea.cur = h->ctr + 1;
-    ea.gz = h->p.bu + h->p.gzbeg;
+    ea.gz = h->rec_xyz.empty() ? h->p.bu + h->p.gzbeg : -1;   // a receiver list records separately
     ea.bl = h->p.bl;
     ea.bf = h->p.bf;
     ea.nx = h->p.nx;
@@ -277,6 +302,7 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = tru
         if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += (n == M ? 36.0 : 44.0) * N; }
         if (e != cudaSuccess) return e;
     }
+    if (source && (e = enqueue_receivers(h, tm)) != cudaSuccess) return e;
     return enqueue_corrector(h, tm);
 }
 
@@ -700,6 +726,39 @@ ose_status ose_get_precision(const ose_handle* h, int* mode)
     return OSE_OK;
 }
 
+ose_status ose_set_receivers(ose_handle* h, int n, const int* xyz)
+{
+    if (!h || n < 0 || (n > 0 && !xyz)) return OSE_ERR_INVALID;
+    const ose_params& p = h->p;
+    for (int i = 0; i < n; ++i) {
+        const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        if (x < 0 || x >= p.nx || y < 0 || y >= p.ny || z < 0 || z >= p.nz)
+            return fail(h, OSE_ERR_INVALID, "receiver " + std::to_string(i) + " outside the model interior");
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    const int ng = n > 0 ? n : p.nx * p.ny;
+    if (ng != h->d.ng) {
+        float* g = nullptr;
+        CK(h, cudaMalloc((void**)&g, sizeof(float) * (size_t)p.nt * ng));
+        cudaFree(h->gather);
+        h->gather = g;
+        h->d.ng = ng;
+    }
+    CK(h, cudaMemset(h->gather, 0, sizeof(float) * (size_t)p.nt * ng));
+    if (h->rec_idx) { cudaFree(h->rec_idx); h->rec_idx = nullptr; }
+    h->rec_xyz.assign(xyz, xyz + 3 * (size_t)n);
+    if (n > 0) {
+        std::vector<long long> idx(n);
+        for (int i = 0; i < n; ++i)
+            idx[i] = ((long long)(p.bu + xyz[3 * i + 2]) * h->d.nyb + (p.bf + xyz[3 * i + 1])) * h->d.nxb +
+                     (p.bl + xyz[3 * i]);
+        CK(h, cudaMalloc((void**)&h->rec_idx, sizeof(long long) * n));
+        CK(h, cudaMemcpy(h->rec_idx, idx.data(), sizeof(long long) * n, cudaMemcpyHostToDevice));
+    }
+    return OSE_OK;
+}
+
 ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
 {
     if (!h) return OSE_ERR_INVALID;
@@ -781,12 +840,12 @@ __global__ void k_take_p(const float2* __restrict__ W, float* __restrict__ snap,
 // Reverse-time injection of one gather row at the receivers (the cells the
 // LAST epilogue records): P += p[ig], Q += q[ig].
 __global__ void k_inject_row(float2* __restrict__ W, const float* __restrict__ p, const float* __restrict__ q, int gz,
-                             int bl, int bf, int nx, int ny, int nxb, int nyb)
+                             int bl, int bf, int nx, int ny, int nxb, int nyb, const long long* __restrict__ idx, int ng)
 {
     const int ig = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ig >= nx * ny) return;
+    if (ig >= ng) return;
     const int iy = ig / nx, ix = ig - iy * nx;
-    float2& w = W[((size_t)gz * nyb + (bf + iy)) * nxb + (bl + ix)];
+    float2& w = W[idx ? idx[ig] : ((size_t)gz * nyb + (bf + iy)) * nxb + (bl + ix)];
     w.x += p[ig];
     w.y += q[ig];
 }
@@ -922,7 +981,8 @@ ose_status ose_rtm(ose_handle* h, const float* rows, int nsteps, int every, floa
     const int gz = h->p.bu + h->p.gzbeg;
     for (int it = nsteps - 1; it >= 0; --it) {
         k_inject_row<<<(ng + 255) / 256, 256, 0, h->stream>>>(h->W, dp + (size_t)it * ng, dq + (size_t)it * ng, gz,
-                                                                h->p.bl, h->p.bf, h->p.nx, h->p.ny, h->d.nxb, h->d.nyb);
+                                                                h->p.bl, h->p.bf, h->p.nx, h->p.ny, h->d.nxb, h->d.nyb,
+                                                                h->rec_xyz.empty() ? nullptr : h->rec_idx, ng);
         CKR(enqueue_step(h, nullptr, false));
         if (it % every == 0)
             k_image<<<blocks, 256, 0, h->stream>>>(img, ill, snaps + N * (size_t)(it / every), h->W, (long long)N);
@@ -1268,6 +1328,8 @@ static ose_status write_traces(ose_handle* h, const char* path, bool segy)
     tg.sz = (double)(p.szbeg + h->shot * p.jsz) * p.dz;
     tg.gz = (double)p.gzbeg * p.dz;
     tg.dt_us = (int)lround((double)p.dt * 1e6);
+    tg.rxyz = h->rec_xyz.empty() ? nullptr : h->rec_xyz.data();
+    tg.dz = p.dz;
     const int rc = ose::write_gather_traces(path, g.data(), tg, segy);
     if (rc == -2) return fail(h, OSE_ERR_UNSUPPORTED, "nt or dt does not fit the 16-bit trace header fields");
     if (rc != 0) return fail(h, OSE_ERR_IO, std::string("cannot write ") + path);

@@ -32,8 +32,9 @@ void put(unsigned char* h, int off, T v, bool big)
 void fill_trace_header(unsigned char* h, const TraceGeometry& g, int ig, bool big)
 {
     memset(h, 0, 240);
-    const int ix = ig % g.nx, iy = ig / g.nx;
+    const int ix = g.rxyz ? g.rxyz[3 * ig] : ig % g.nx, iy = g.rxyz ? g.rxyz[3 * ig + 1] : ig / g.nx;
     const double gx = (double)ix * g.dx, gy = (double)iy * g.dy;
+    const double gzr = g.rxyz ? (double)g.rxyz[3 * ig + 2] * g.dz : g.gz;
     const double ox = gx - g.sx, oy = gy - g.sy;
     const int32_t scale = -100;   // coordinates stored in centimetres (value / 100)
     put<int32_t>(h, 0, ig + 1, big);                    // tracl
@@ -43,7 +44,7 @@ void fill_trace_header(unsigned char* h, const TraceGeometry& g, int ig, bool bi
     put<int32_t>(h, 16, g.shot + 1, big);               // ep
     put<int16_t>(h, 28, 1, big);                        // trid: seismic data
     put<int32_t>(h, 36, (int32_t)(100.0 * sqrt(ox * ox + oy * oy) + 0.5), big);  // offset
-    put<int32_t>(h, 40, (int32_t)(-100.0 * g.gz + (g.gz >= 0 ? -0.5 : 0.5)), big);       // gelev
+    put<int32_t>(h, 40, (int32_t)(-100.0 * gzr + (gzr >= 0 ? -0.5 : 0.5)), big);         // gelev
     put<int32_t>(h, 48, (int32_t)(100.0 * g.sz + 0.5), big);                               // sdepth
     put<int16_t>(h, 68, (int16_t)scale, big);           // scalel
     put<int16_t>(h, 70, (int16_t)scale, big);           // scalco

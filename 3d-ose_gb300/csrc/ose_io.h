@@ -11,6 +11,9 @@ struct TraceGeometry {
     double sx, sy, sz;     // source position
     double gz;             // receiver depth
     int dt_us;             // sample interval in microseconds
+    const int* rxyz;       // receiver list: (x, y, z) interior cells per trace, or
+                           // null for the receiver plane (ig = iy * nx + ix, depth gz)
+    double dz;
 };
 
 // Writes ng traces of nt samples from gather_ig_it ([ig][it]); segy = false

@@ -44,7 +44,7 @@ EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_fr
            "ose_corrector_last_error", "ose_corrector_info", "ose_corrector_set_params",
            "ose_corrector_get_params", "ose_corrector_get_grads", "ose_corrector_forward",
            "ose_corrector_apply", "ose_corrector_train_sample", "ose_corrector_adam", "ose_corrector_loss",
-           "ose_rtm", "ose_batch_set_tuning"]
+           "ose_rtm", "ose_batch_set_tuning", "ose_set_receivers"]
 CORRECTOR_SHELL = 16   # OSE_CORRECTOR_SHELL
 
 # void (*)(int it, const float* P, const float* Q, void* user)
@@ -124,6 +124,7 @@ def load_library(path: str = LIB_PATH):
         "ose_set_precision": ([H, ctypes.c_int], ctypes.c_int),
         "ose_set_corrector": ([H, f32, ctypes.c_int], ctypes.c_int),
         "ose_rtm": ([H, f32, ctypes.c_int, ctypes.c_int, f32, f32], ctypes.c_int),
+        "ose_set_receivers": ([H, ctypes.c_int, P(ctypes.c_int)], ctypes.c_int),
         "ose_state_box": ([H, ctypes.c_int, P(ctypes.c_int), ctypes.c_void_p, P(ctypes.c_int)], ctypes.c_int),
         "ose_corrector_param_count": ([], ctypes.c_size_t),
         "ose_corrector_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), P(H)],
@@ -212,6 +213,13 @@ class ShotWindow(ctypes.Structure):
     """ose_shot_window (include/ose3d.h)."""
 
     _fields_ = [(k, ctypes.c_int) for k in ("x0", "y0", "z0", "nx", "ny", "nz", "sx", "sy", "sz")]
+
+
+def receiver_line(gxbeg: int, gybeg: int, gzbeg: int, jgx: int, jgy: int, jgz: int, n: int) -> np.ndarray:
+    """The reference's receiver geometry (sg_init_device): receiver i at
+    (gxbeg + i jgx, gybeg + i jgy, gzbeg + i jgz), i < n."""
+    i = np.arange(n)
+    return np.stack([gxbeg + i * jgx, gybeg + i * jgy, gzbeg + i * jgz], axis=1).astype(np.int32)
 
 
 class Corrector:
@@ -516,6 +524,17 @@ class Modeler:
             return
         p = np.ascontiguousarray(params, np.float32)
         self._check(self._lib.ose_set_corrector(self._h, _f32(p), shell))
+
+    def set_receivers(self, xyz):
+        """Receivers at explicit interior cells (n x 3 array of x, y, z), or
+        None for the receiver plane at depth gzbeg."""
+        if xyz is None or len(xyz) == 0:
+            self._check(self._lib.ose_set_receivers(self._h, 0, None))
+        else:
+            a = np.ascontiguousarray(np.asarray(xyz, dtype=np.int32).reshape(-1, 3))
+            self._check(self._lib.ose_set_receivers(self._h, a.shape[0],
+                                                    a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        self._check(self._lib.ose_get_derived(self._h, ctypes.byref(self.derived)))
 
     def rtm(self, rows: np.ndarray, every: int = 4):
         """Reverse-time migration of the current shot's observed receiver rows

@@ -181,6 +181,16 @@ enum {
 ose_status ose_set_precision(ose_handle* h, int mode);
 ose_status ose_get_precision(const ose_handle* h, int* mode);
 
+/* Receivers at an explicit list of interior cells (xyz: n triplets x, y, z,
+ * 0-based interior coordinates) instead of the plane at depth gzbeg.  This is
+ * the reference's gxyz geometry (sg_init_device, ose_3d_kernel.cu:202-212:
+ * receiver i at (gxbeg + i jgx, gybeg + i jgy, gzbeg + i jgz)), which its
+ * rec_shotdata_3d leaves unused in favour of the full surface plane
+ * (ose_3d_kernel.cu:412-436); here it is honoured.  ng becomes n; the gather,
+ * SU/SEG-Y headers and reverse-time migration follow the list.  n = 0 returns
+ * to the plane.  Clears the gather. */
+ose_status ose_set_receivers(ose_handle* h, int n, const int* xyz);
+
 /* ---- learned boundary corrector (no counterpart in the reference) --------
  * A 3D convolutional network (4 layers of 3x3x3 convolutions, 8 -> 32 -> 32
  * -> 32 -> 2 channels, ReLU, ose_corrector_param_count() FP32 parameters)
