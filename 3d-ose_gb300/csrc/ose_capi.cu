@@ -323,17 +323,19 @@ ose_status build_graph(ose_handle* h)
 
 ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVALID; }
 
-// After the stream is idle: the tensor-core z pass records a wait that ran out
-// of time in its error word (the kernel then leaves its columns unchanged).
+// After the stream is idle: kernels with bounded waits (tensor-core z pass,
+// corrector, the plane path's exchange) record a wait that ran out of time
+// in the handle's error word.
 ose_status tensor_status(ose_handle* h)
 {
-    if ((h->precision == OSE_PRECISION_FP32 && !h->corr) || !h->tcerr) return OSE_OK;
+    if (!h->tcerr) return OSE_OK;
     int v = 0;
     CK(h, cudaMemcpy(&v, h->tcerr, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
         CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
-        return fail(h, OSE_ERR_CUDA, v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
-                                            : "tensor-core z pass: an MMA completion wait ran out of time");
+        return fail(h, OSE_ERR_CUDA, v == 3 ? "plane exchange: an mbarrier wait ran out of time"
+                                     : v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
+                                              : "tensor-core z pass: an MMA completion wait ran out of time");
     }
     return OSE_OK;
 }
@@ -508,6 +510,8 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(dalloc(h, &h->hil, (size_t)p.nt));
     CKC(dalloc(h, &h->gather, (size_t)p.nt * d.ng));
     CKC(dalloc(h, &h->ctr, 4));
+    CKC(dalloc(h, &h->tcerr, 1));
+    CKC(cudaMemset(h->tcerr, 0, sizeof(int)));
     if (ose::kCompensatedConstants) {
         CKC(upload(h, h->vs, h->vb));
     } else {
@@ -540,6 +544,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     h->tables.ky2 = h->ky2;
     h->tables.kz2 = h->kz2;
     h->tables.twl = h->twxl;
+    h->tables.tcerr = h->tcerr;
     h->tables.kx2l = h->kx2l;
     h->tables.ky2l = h->ky2l;
     h->tables.kz2l = h->kz2l;
