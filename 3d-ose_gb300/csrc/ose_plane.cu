@@ -44,10 +44,7 @@ constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buf
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
 constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N;   // + twiddle table (hi, lo)
-// after the complex data: two mbarriers of the forward exchange (receive, ready)
-constexpr size_t BAR_OFF = sizeof(float2) * SMEM_COMPLEX;
-constexpr size_t SMEM_BYTES = BAR_OFF + 16;
-constexpr uint64_t kWaitLimitNs = 1000000000ull;
+constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX;
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -218,70 +215,6 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
     dft16<INV>(v1);
 }
 
-// Distributed shared memory and mbarrier primitives of the forward exchange.
-__device__ __forceinline__ uint32_t s_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// This CTA's shared address a as seen in CTA `rank` of the cluster.
-__device__ __forceinline__ uint32_t mapa(uint32_t a, uint32_t rank)
-{
-    uint32_t r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-    return r;
-}
-
-__device__ __forceinline__ void bar_init(uint32_t a, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-
-// Arrive once and expect `bytes` of st.async data in this phase.
-__device__ __forceinline__ void bar_expect_tx(uint32_t a, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
-}
-
-// Arrive on an mbarrier of another CTA, without ordering this CTA's memory
-// operations (a readiness signal, not a data release).
-__device__ __forceinline__ void bar_arrive_remote(uint32_t ra)
-{
-    asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(ra) : "memory");
-}
-
-// 8 bytes into another CTA's shared memory; completes 8 bytes of the
-// transaction count of that CTA's mbarrier rbar.
-__device__ __forceinline__ void st_async(uint32_t ra, float2 v, uint32_t rbar)
-{
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(ra),
-                 "f"(v.x), "f"(v.y), "r"(rbar)
-                 : "memory");
-}
-
-__device__ __forceinline__ uint64_t now_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Phase `parity` of a local mbarrier, acquiring what other CTAs of the
-// cluster wrote into it; false after kWaitLimitNs.
-__device__ __forceinline__ bool bar_wait_cluster(uint32_t a, uint32_t parity)
-{
-    const uint64_t t0 = now_ns();
-    for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (now_ns() - t0 > kWaitLimitNs) return false;
-    }
-}
-
 struct Args {
     const float2* src;     // k_plane_fwd: state rows.  k_plane_inv: spectrum after k_zpass
     float2* dst;           // spectrum of the next application (forward output)
@@ -290,21 +223,8 @@ struct Args {
     const float* kx2;
     const float* ky2;
     const float* kz2;
-    int* err;              // device error word: 3 = an exchange wait ran out of time
     EpiArgs e;
 };
-
-// mbarriers of the forward exchange, initialised by thread 0 at kernel start
-// (made visible to the cluster by the kernel's first cluster barrier).
-__device__ __forceinline__ void init_exchange_bars(float2* smem)
-{
-    if (threadIdx.x == 0) {
-        uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(smem) + BAR_OFF);
-        bar_init(s_u32(bars), 1);        // receive: one local arrive + the transaction bytes
-        bar_init(s_u32(bars + 1), CL);   // ready: one arrive from every CTA of the cluster
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-}
 
 // W_256^t, t < 256, at tw[t] (nearest floats) and tw[256 + t] (remainders)
 __device__ __forceinline__ void load_twiddles(float2* tw, const float2* g, const float2* gl)
@@ -324,55 +244,33 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
 
 // Forward x FFT of this CTA's 32 rows (values in v0/v1, spatial order) then
 // forward y FFT of its 32 columns; spectrum stored to dst plane z.
-// The rows change hands by push: every CTA writes each value straight into
-// the shared memory of the CTA that owns its column (st.async, counted by the
-// receiver's mbarrier), once that CTA has signalled that its buffer is free.
-// No cluster barrier, so nothing waits for the epilogue's global stores.
-__device__ __forceinline__ void forward_xy(float2* smem, const float2* tw, float2 (&v0)[16], float2 (&v1)[16],
-                                           float2* dst, int z, int r, int* err)
+__device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* smem, const float2* tw,
+                                           float2 (&v0)[16], float2 (&v1)[16], float2* dst, int z, int r)
 {
     float2* T = smem;
     fft256<false, true>(T, tw, v0, v1);
-    // fft256 ended with a barrier: this CTA's buffer is free
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(smem) + BAR_OFF);
-    const uint32_t recv = s_u32(bars), ready = s_u32(bars + 1);
-    if (threadIdx.x == 0) {
-        bar_expect_tx(recv, (uint32_t)(SL * N * sizeof(float2)));   // 32 columns x 256 rows
+    // natural-order rows into this CTA's slice A[row][kx]
+    float2* A = smem;
 #pragma unroll
-        for (int q = 0; q < CL; ++q) bar_arrive_remote(mapa(ready, q));
+    for (int s = 0; s < 2; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) A[q.row * N + q.j + 16 * k2] = v[k2];
     }
-    int bad = 0;
-    if (threadIdx.x == 0) bad = !bar_wait_cluster(ready, 0);   // every receiver is ready
-    bad = __syncthreads_or(bad);
-    // row y, column kx -> CTA kx / 32, buffer B[y][kx % 32]
-    const uint32_t B = s_u32(smem);
-#pragma unroll
-    for (int o = 0; o < CL; ++o) {   // owner o takes k2 = 2 o, 2 o + 1
-        const uint32_t rb = mapa(B, o), rbar = mapa(recv, o);
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const RowSlot q = row_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-            const int y = SL * r + q.row;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int k2 = 2 * o + h, kx = q.j + 16 * k2;   // column kx % 32 of owner o
-                st_async(rb + (uint32_t)((y * SL + (kx & (SL - 1))) * sizeof(float2)), v[k2], rbar);
-            }
-        }
-    }
-    if (!bar_wait_cluster(recv, 0)) bad = 1;   // this CTA's 64 KiB have arrived
-    if (bad && err) atomicExch(err, 3);
-    // columns 32r..32r+31 of all 256 rows
-    const float2* Bb = smem;
+    cluster.sync();
+    // columns 32r..32r+31 of all 256 rows from the 8 slices
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) v[n1] = Bb[(16 * n1 + q.j) * SL + q.c];
+        for (int n1 = 0; n1 < 16; ++n1) {
+            const float2* rem = cluster.map_shared_rank(A, n1 >> 1);
+            v[n1] = rem[((16 * n1 + q.j) & (SL - 1)) * N + SL * r + q.c];
+        }
     }
-    __syncthreads();   // the buffer becomes fft256's exchange buffer
+    cluster.sync();
     fft256<false, false>(T, tw, v0, v1);
     float2* out = dst + (size_t)z * N * N + SL * r;
 #pragma unroll
@@ -393,8 +291,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
     load_twiddles(tw, a.tw, a.twl);
-    init_exchange_bars(smem);
-    cluster.sync();   // the exchange mbarriers are initialised cluster-wide
     float2 v0[16], v1[16];
     const float2* in = a.src + ((size_t)z * N + SL * r) * N;
 #pragma unroll
@@ -405,7 +301,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
         for (int n1 = 0; n1 < 16; ++n1) v[n1] = in[(size_t)q.row * N + 16 * n1 + q.j];
     }
     __syncthreads();
-    forward_xy(smem, tw, v0, v1, a.dst, z, r, a.err);
+    forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
@@ -513,7 +409,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
         }
     }
     load_twiddles(tw, a.tw, a.twl);
-    if (FWD) init_exchange_bars(smem);
     float2 v0[16], v1[16];
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
     const float2* in = a.src + (size_t)z * N * N + SL * r;
@@ -554,7 +449,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     // pointwise update on (x = 16 n1 + j, y, z)
     epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
     epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
-    if (FWD) forward_xy(smem, tw, v0, v1, a.dst, z, r, a.err);
+    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
 // z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
@@ -671,7 +566,6 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
     a.dst = X;
     a.tw = t.twx;
     a.twl = t.twl;
-    a.err = t.tcerr;
     plane::k_plane_fwd<<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
     return cudaGetLastError();
 }
@@ -696,7 +590,6 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     a.dst = Xout;
     a.tw = t.twx;
     a.twl = t.twl;
-    a.err = t.tcerr;
     a.e = e;
     const dim3 grid(plane::CL, plane::N);
     if (mode == EPI_FIRST)
