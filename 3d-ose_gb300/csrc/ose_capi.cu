@@ -179,20 +179,25 @@ cudaError_t enqueue_receivers(ose_handle* h, ose::KernelTiming* tm)
     });
 }
 
-// The learned boundary correction at the end of a step (timing class 6;
-// bytes: the shell's features, three hidden layers and the state update).
+// The learned boundary correction at the end of a step: timing class 6 the
+// local scale (shell sum of squares, three box passes over the grid), class 7
+// the four layers (bytes: layer 0 reads state + velocity + scale and writes
+// 32 BF16 channels, two hidden layers read and write them, the output layer
+// reads them and updates the state).
 cudaError_t enqueue_corrector(ose_handle* h, ose::KernelTiming* tm)
 {
     if (!h->corr) return cudaSuccess;
     const ose::learn::Net& n = ose::learn::net_of(h->corr);
     const ose::learn::TcNet* tc = ose::learn::tc_of(h->corr);
-    // shell bytes: scale read, layer 0 reads state + velocity and writes 32
-    // BF16 channels, two hidden layers read and write them, the output layer
-    // reads them and updates the state
+    const double grid = (double)n.g.nx * n.g.ny * n.g.nz;
+    cudaError_t e = timed(tm, h->stream, 6, (double)n.ncells * 8.0 + grid * (8.0 + 5 * 4.0), [&] {
+        return ose::learn::shell_scale(h->stream, n, h->W);
+    });
+    if (e != cudaSuccess) return e;
     const double bytes = (double)n.ncells * (8.0 + 12.0 + 64.0 + 2 * 128.0 + 64.0 + 16.0);
-    return timed(tm, h->stream, 6, bytes, [&] {
-        return tc ? ose::learn::forward_tc(h->stream, n, *tc, h->W, h->corr_vel)
-                  : ose::learn::forward(h->stream, n, h->W, h->corr_vel, true, h->W);
+    return timed(tm, h->stream, 7, bytes, [&] {
+        return tc ? ose::learn::forward_tc(h->stream, n, *tc, h->W, h->corr_vel, false)
+                  : ose::learn::forward(h->stream, n, h->W, h->corr_vel, true, h->W, false);
     });
 }
 
@@ -1100,11 +1105,11 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
     if (h->it + reps > h->p.nt) return fail(h, OSE_ERR_INVALID, "reps beyond nt");
     ose::KernelTiming& t = h->timing;
     static const char* kGeneric[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
-                                     "fft_x_inv_epilogue", "inject", "corrector"};
+                                     "fft_x_inv_epilogue", "inject", "corrector_scale", "corrector"};
     static const char* kPlane[] = {"plane_fwd", "zpass", "plane_inv_first", "plane_inv_mid",
-                                   "plane_inv_last", "inject", "corrector"};
+                                   "plane_inv_last", "inject", "corrector_scale", "corrector"};
     const char** kNames = h->d.path == OSE_PATH_PLANE ? kPlane : kGeneric;
-    const int nc = h->corr ? 7 : 6;
+    const int nc = h->corr ? 8 : 6;
     for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
     for (int r = 0; r < reps; ++r) {
         CK(h, enqueue_step(h, &t));

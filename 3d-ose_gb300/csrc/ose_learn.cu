@@ -103,67 +103,61 @@ __global__ void k_shell_scale(float* scal, float inv_count2)
 }
 
 // Local scale s(x): three periodic box sums of P^2 + Q^2 (shell cells) with
-// half-width kBoxR, x then y then z over the whole padded grid.  Each thread
-// slides the window along one whole line (one add and one subtract per cell).
+// half-width kBoxR, x then y then z over the whole padded grid.  Each pass
+// stages whole lines in shared memory (coalesced global reads and writes)
+// and every output is a 17-term sum from shared memory.
 constexpr int kBoxR = 8;
+constexpr int kBoxTX = 32;   // x columns per block of the y and z passes
 
 __device__ __forceinline__ int modi(int v, int n) { return ((v % n) + n) % n; }
 
-__device__ __forceinline__ float shell_energy(const float2* __restrict__ W, const NetGeom& g, int x, int y, int z)
-{
-    if (!in_shell(g, x, y, z)) return 0.f;
-    const float2 w = W[((size_t)z * g.ny + y) * g.nx + x];
-    return fmaf(w.x, w.x, w.y * w.y);
-}
-
-// thread per (y, z) row
+// block per (y, z) row; e[x] with its periodic halo in shared memory
 __global__ void k_box_x(const float2* __restrict__ W, float* __restrict__ out, NetGeom g)
 {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= g.ny * g.nz) return;
-    const int y = row % g.ny, z = row / g.ny;
-    float acc = 0.f;
-    for (int d = -kBoxR; d <= kBoxR; ++d) acc += shell_energy(W, g, modi(d, g.nx), y, z);
+    extern __shared__ float box_e[];   // [nx + 2 kBoxR]
+    const int row = blockIdx.x, y = row % g.ny, z = row / g.ny;
+    const float2* w = W + (size_t)row * g.nx;
+    for (int j = threadIdx.x; j < g.nx + 2 * kBoxR; j += blockDim.x) {
+        const int x = modi(j - kBoxR, g.nx);
+        const float2 v = w[x];
+        box_e[j] = in_shell(g, x, y, z) ? fmaf(v.x, v.x, v.y * v.y) : 0.f;
+    }
+    __syncthreads();
     float* o = out + (size_t)row * g.nx;
-    for (int x = 0; x < g.nx; ++x) {
+    for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+        float acc = 0.f;
+        for (int d = 0; d <= 2 * kBoxR; ++d) acc += box_e[x + d];
         o[x] = acc;
-        acc += shell_energy(W, g, modi(x + kBoxR + 1, g.nx), y, z) - shell_energy(W, g, modi(x - kBoxR, g.nx), y, z);
     }
 }
 
-// thread per (x, z) line along y
-__global__ void k_box_y(const float* __restrict__ in, float* __restrict__ out, NetGeom g)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.nx * g.nz) return;
-    const int x = t % g.nx, z = t / g.nx;
-    const float* a = in + (size_t)z * g.ny * g.nx + x;
-    float* o = out + (size_t)z * g.ny * g.nx + x;
-    float acc = 0.f;
-    for (int d = -kBoxR; d <= kBoxR; ++d) acc += a[(size_t)modi(d, g.ny) * g.nx];
-    for (int y = 0; y < g.ny; ++y) {
-        o[(size_t)y * g.nx] = acc;
-        acc += a[(size_t)modi(y + kBoxR + 1, g.ny) * g.nx] - a[(size_t)modi(y - kBoxR, g.ny) * g.nx];
-    }
-}
+// block per (x tile, plane index, chunk of kBoxL outputs): lines of length n
+// at stride `stride` (y pass: n = ny, stride nx, plane = z; z pass: n = nz,
+// stride nx ny, plane = y); the chunk and its periodic halo sit in shared
+// memory.  FINAL: s = sqrt(m / 2 + f^2), m the box mean, f = 1e-3 x the shell
+// RMS.
+constexpr int kBoxL = 256;
 
-// thread per (x, y) line along z, then s = sqrt(m / 2 + f^2) with m the box
-// mean and f = 1e-3 x the shell RMS.
-__global__ void k_box_z(const float* __restrict__ in, float* __restrict__ sloc, const float* __restrict__ scal,
-                        NetGeom g)
+template <bool FINAL>
+__global__ void __launch_bounds__(256) k_box_lines(const float* __restrict__ in, float* __restrict__ out,
+                                                   const float* __restrict__ scal, int n, long long stride,
+                                                   long long pstride, int nx)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.nx * g.ny) return;
-    const size_t plane = (size_t)g.nx * g.ny;
-    const float f = 1e-3f * scal[1];
+    __shared__ float box_e[(kBoxL + 2 * kBoxR) * kBoxTX];
+    const int c = threadIdx.x, x = blockIdx.x * kBoxTX + c;
+    const int i0 = blockIdx.z * kBoxL, len = min(kBoxL, n - i0);
+    const size_t base = (size_t)blockIdx.y * pstride + x;
+    const bool ok = x < nx;
+    for (int j = threadIdx.y; j < len + 2 * kBoxR; j += blockDim.y)
+        box_e[j * kBoxTX + c] = ok ? in[base + (size_t)modi(i0 + j - kBoxR, n) * stride] : 0.f;
+    __syncthreads();
+    if (!ok) return;
+    const float f = FINAL ? 1e-3f * scal[1] : 0.f;
     const float inv_vol = 1.f / (float)((2 * kBoxR + 1) * (2 * kBoxR + 1) * (2 * kBoxR + 1));
-    const float* a = in + t;
-    float* o = sloc + t;
-    float acc = 0.f;
-    for (int d = -kBoxR; d <= kBoxR; ++d) acc += a[(size_t)modi(d, g.nz) * plane];
-    for (int z = 0; z < g.nz; ++z) {
-        o[(size_t)z * plane] = sqrtf(0.5f * fmaxf(acc, 0.f) * inv_vol + f * f);
-        acc += a[(size_t)modi(z + kBoxR + 1, g.nz) * plane] - a[(size_t)modi(z - kBoxR, g.nz) * plane];
+    for (int j = threadIdx.y; j < len; j += blockDim.y) {
+        float acc = 0.f;
+        for (int d = 0; d <= 2 * kBoxR; ++d) acc += box_e[(j + d) * kBoxTX + c];
+        out[base + (size_t)(i0 + j) * stride] = FINAL ? sqrtf(0.5f * fmaxf(acc, 0.f) * inv_vol + f * f) : acc;
     }
 }
 
@@ -512,18 +506,23 @@ cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
     k_shell_sumsq<<<gr, 256, 0, s>>>(W, n.g, n.tiles, n.ntiles, n.scal);
     k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
     const NetGeom& g = n.g;
-    k_box_x<<<(g.ny * g.nz + 127) / 128, 128, 0, s>>>(W, n.sloc, g);
-    k_box_y<<<(g.nx * g.nz + 127) / 128, 128, 0, s>>>(n.sloc, n.stmp, g);
-    k_box_z<<<(g.nx * g.ny + 127) / 128, 128, 0, s>>>(n.stmp, n.sloc, n.scal, g);
+    const long long plane = (long long)g.nx * g.ny;
+    const unsigned xt = (unsigned)((g.nx + kBoxTX - 1) / kBoxTX);
+    k_box_x<<<g.ny * g.nz, 256, sizeof(float) * (g.nx + 2 * kBoxR), s>>>(W, n.sloc, g);
+    k_box_lines<false><<<dim3(xt, g.nz, (g.ny + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
+        n.sloc, n.stmp, n.scal, g.ny, g.nx, plane, g.nx);
+    k_box_lines<true><<<dim3(xt, g.ny, (g.nz + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
+        n.stmp, n.sloc, n.scal, g.nz, plane, g.nx, g.nx);
     return cudaGetLastError();
 }
 
-cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out)
+cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out,
+                    bool scale)
 {
     const NetGeom& g = n.g;
     const float* p = n.params;
     const unsigned gr = grid_for(n.ntiles, 2);
-    cudaError_t e0 = shell_scale(s, n, W);
+    cudaError_t e0 = scale ? shell_scale(s, n, W) : cudaSuccess;
     if (e0 != cudaSuccess) return e0;
     k_features<<<gr, 256, 0, s>>>(W, vel, n.sloc, n.F, g, n.tiles, n.ntiles);
     const float* w0 = p + param_offset(0);
@@ -680,7 +679,7 @@ cudaError_t create_tc(ose_corrector* c, const float* params_host, int* err)
     TcNet& t = c->tc;
     std::vector<int> tiles;
     tc_tiles(c->net.g, tiles);
-    t.ntiles = (int)tiles.size();
+    t.ntiles = (int)tiles.size() / 2;   // columns of (x, y) tile, z0, planes
     const size_t cells = (size_t)c->net.g.nx * c->net.g.ny * c->net.g.nz;
     cudaError_t e;
     if ((e = corr_alloc(c, &t.tiles, tiles.size(), false)) != cudaSuccess) return e;

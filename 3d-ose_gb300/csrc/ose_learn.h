@@ -49,7 +49,8 @@ struct Net {
 
 // Tensor-core inference (ose_learn_tc.cu): BF16 weights per layer in the
 // kernel's shared-memory layout, biases padded to the layer's N, BF16
-// ping-pong activations [cell][32], and the 8 x 16 x 1 output tiles.
+// ping-pong activations [cell][32], and the columns of 8 x 16 output planes
+// (two ints each: x tile | y tile << 10, z0 | planes << 16).
 struct TcNet {
     int* tiles;
     int ntiles;
@@ -65,7 +66,9 @@ void shell_tiles(const NetGeom& g, std::vector<int>& tiles, long long* ncells, l
 cudaError_t configure();
 // Forward pass on state W (float2 P + iQ, [z][y][x]) and velocity vel.  With
 // apply, adds the correction to state_out (may equal W); else writes n.O.
-cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out);
+// scale = false: n.sloc / n.scal already hold this state's local scale
+cudaError_t forward(cudaStream_t s, const Net& n, const float2* W, const float* vel, bool apply, float2* state_out,
+                    bool scale = true);
 // Forward + backward of one sample; gradients add into n.grads, loss into n.loss.
 cudaError_t train_sample(cudaStream_t s, const Net& n, const float2* W, const float* vel, const float2* tgt);
 // One Adam update with gradients scaled by gscale; clears the gradients.
@@ -77,7 +80,8 @@ void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, 
 void tc_tiles(const NetGeom& g, std::vector<int>& tiles);
 cudaError_t configure_tc();
 // state += s * corrector(state) at the write cells, on the tensor cores.
-cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel);
+cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel,
+                       bool scale = true);
 
 // Corrector objects (the C ABI's ose_corrector) for the modeler's own use.
 ose_corrector* new_corrector();

@@ -2,15 +2,18 @@
 // cores: each 3x3x3 convolution layer is an implicit GEMM with BF16 weights
 // and activations and an FP32 accumulator in TMEM.
 //
-// A CTA computes output tiles of 8 (x) x 16 (y) x 1 (z) = 128 cells, the M
-// rows of the MMA (row m = y * 8 + x).  It stages the input halo of the tile,
-// 10 x 18 x 3 cells with all input channels, once in shared memory in the
-// layout [z 3][y 18][channel chunk][x 10][8 channels x 2 bytes]: for a tap
-// (dx, dy, dz) the 128 x Cin operand is then a plain K-major descriptor into
-// the halo (rows 16 bytes apart, y groups SBO apart, channel chunks LBO apart,
-// start shifted by dx * 16 bytes), so no im2col copy is made.  A tile is
-// 27 taps x Cin / 16 MMAs of 128 x N x 16 (N = 32, or 16 for the 2-channel
-// output layer padded with zero weights), accumulated in TMEM.
+// A CTA walks a column of output planes: 8 (x) x 16 (y) cells, the M rows of
+// the MMA (row m = y * 8 + x), for up to ZL consecutive z.  The input halo
+// planes (10 x 18 cells, all input channels) sit in a ring of four shared-
+// memory slots, each in the layout [y 18][channel chunk][x 10][8 channels x
+// 2 bytes]: for a tap (dx, dy, dz) the 128 x Cin operand is a plain K-major
+// descriptor into the slot of plane z + dz (rows 16 bytes apart, y groups SBO
+// apart, channel chunks LBO apart, start shifted by dx * 16 bytes), so no
+// im2col copy is made.  An output plane is 27 taps x Cin / 16 MMAs of
+// 128 x N x 16 (N = 32, or 16 for the 2-channel output layer padded with zero
+// weights), accumulated in TMEM.  Moving one plane along z loads one new halo
+// plane (180 cells for 128 outputs), and its global loads are in flight while
+// the CTA waits for the previous plane's MMAs and writes its outputs.
 //
 // Layer 0's halo is built from the state and the velocity (the 8 features,
 // padded to 16 channels with zeros); hidden activations are BF16 [cell][32];
@@ -33,8 +36,10 @@ namespace learn {
 
 namespace {
 
-constexpr int TXW = 8, TYW = 16;              // output tile (x, y), one z plane
-constexpr int HX = TXW + 2, HY = TYW + 2, HZ = 3;
+constexpr int TXW = 8, TYW = 16;              // output tile (x, y) of one z plane
+constexpr int HX = TXW + 2, HY = TYW + 2;
+constexpr int ZL = 16;                        // output planes per column at most
+constexpr int SLOTS = 4;                      // ring of halo planes
 constexpr int THREADS = 128;                  // one output row (cell) per thread
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
 
@@ -71,9 +76,10 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
 template <int CIN, int NPAD>
 struct LayerCfg {
     static constexpr int chunks = CIN / 8;                       // 16-byte channel chunks
-    static constexpr int halo_bytes = HZ * HY * chunks * HX * 16;
-    static constexpr uint32_t lbo = HX * 16;                     // chunk stride in the halo
-    static constexpr uint32_t sbo = chunks * HX * 16;            // y stride in the halo
+    static constexpr int plane_bytes = HY * chunks * HX * 16;    // one halo plane
+    static constexpr int halo_bytes = SLOTS * plane_bytes;
+    static constexpr uint32_t lbo = HX * 16;                     // chunk stride in a plane
+    static constexpr uint32_t sbo = chunks * HX * 16;            // y stride in a plane
     static constexpr int ngroups = NPAD / 8;
     static constexpr int w_bytes = 27 * ngroups * chunks * 128;  // B operands, all taps
     static constexpr uint32_t wsbo = chunks * 128;               // B: n-group stride
@@ -83,19 +89,84 @@ struct LayerCfg {
     static constexpr int off_bar = off_bias + NPAD * 4;
     static constexpr int smem = off_bar + 16;
     static constexpr uint32_t id = tc5::idesc(tc5::kTypeBF16, 128, NPAD);
+    // staged loads of one halo plane per thread: cells (layer 0) or 16-byte units
+    static constexpr int cells = HY * HX;
+    static constexpr int units = cells * chunks;
+    static constexpr int per = ((CIN == 16 ? cells : units) + THREADS - 1) / THREADS;
 };
+
+// One halo plane in registers: layer 0 keeps the state, velocity and scale of
+// each cell; the other layers keep 16-byte units of BF16 activations.
+template <int MODE, int PER>
+struct Staged {
+    float2 w[MODE == 0 ? PER : 1];
+    float v[MODE == 0 ? PER : 1], s[MODE == 0 ? PER : 1];
+    uint4 u[MODE == 0 ? 1 : PER];
+    bool ok[PER];
+};
+
+template <int CIN, int NPAD, int MODE>
+__device__ __forceinline__ void load_plane(Staged<MODE, LayerCfg<CIN, NPAD>::per>& st, const uint16_t* act_in,
+                                           const float2* Win, const float* vel, const float* scal,
+                                           const NetGeom& g, int x0, int y0, int z, int t)
+{
+    using C = LayerCfg<CIN, NPAD>;
+#pragma unroll
+    for (int k = 0; k < C::per; ++k) {
+        const int u = t + k * THREADS;
+        const int ch = MODE == 0 ? 0 : u % C::chunks, cell = MODE == 0 ? u : u / C::chunks;
+        const int hx = cell % HX, hy = cell / HX;
+        const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny);
+        const bool ok = u < (MODE == 0 ? C::cells : C::units) && in_shell(g, x, y, z);
+        const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+        st.ok[k] = ok;
+        if (MODE == 0) {
+            st.w[k] = ok ? __ldg(Win + c) : make_float2(0.f, 0.f);
+            st.v[k] = ok ? __ldg(vel + c) : 0.f;
+            st.s[k] = ok ? __ldg(scal + c) : 1.f;
+        } else {
+            st.u[k] = ok ? __ldg(reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8)) : make_uint4(0, 0, 0, 0);
+        }
+    }
+}
+
+template <int CIN, int NPAD, int MODE>
+__device__ __forceinline__ void store_plane(const Staged<MODE, LayerCfg<CIN, NPAD>::per>& st, uint8_t* slot,
+                                            const NetGeom& g, int x0, int y0, int z, int t)
+{
+    using C = LayerCfg<CIN, NPAD>;
+#pragma unroll
+    for (int k = 0; k < C::per; ++k) {
+        const int u = t + k * THREADS;
+        if (u >= (MODE == 0 ? C::cells : C::units)) break;
+        const int ch = MODE == 0 ? 0 : u % C::chunks, cell = MODE == 0 ? u : u / C::chunks;
+        const int hx = cell % HX, hy = cell / HX;
+        uint4 v = MODE == 0 ? make_uint4(0, 0, 0, 0) : st.u[k];
+        if (MODE == 0 && st.ok[k]) {
+            const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny);
+            const float inv = 1.f / st.s[k];
+            v.x = pack2(st.w[k].x * inv, st.w[k].y * inv);
+            v.y = pack2(st.v[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
+            v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
+        }
+        *reinterpret_cast<uint4*>(slot + ((hy * C::chunks + ch) * HX + hx) * 16) = v;
+        if (MODE == 0)   // channels 8..15 of layer 0 are zero padding
+            *reinterpret_cast<uint4*>(slot + ((hy * C::chunks + 1) * HX + hx) * 16) = make_uint4(0, 0, 0, 0);
+    }
+}
 
 // MODE 0: layer 0 (features from state + velocity), hidden output (ReLU, BF16)
 // MODE 1: hidden layer, BF16 in, hidden output
 // MODE 2: output layer, BF16 in, state += s(x) (o0, o1) at the write cells
-// (scal = the local scale s(x) per cell)
+// (scal = the local scale s(x) per cell).  cols: (x tile | y tile << 10,
+// z0 | planes << 16) per column.
 template <int CIN, int NPAD, int MODE>
 __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict__ act_in,
                                                      const float2* __restrict__ Win, const float* __restrict__ vel,
                                                      const uint8_t* __restrict__ wts, const float* __restrict__ bias,
                                                      uint16_t* __restrict__ act_out, float2* __restrict__ state,
                                                      const float* __restrict__ scal, NetGeom g,
-                                                     const int* __restrict__ tiles, int ntiles, int* err)
+                                                     const int2* __restrict__ cols, int ncols, int* err)
 {
     using C = LayerCfg<CIN, NPAD>;
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -120,94 +191,11 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     int failed = 0;
     uint32_t phase = 0;
+    Staged<MODE, C::per> st;
 
-    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-        const int tp = tiles[tile];
-        const int x0 = (tp & 1023) * TXW, y0 = ((tp >> 10) & 1023) * TYW, z0 = tp >> 20;
-        // halo: HZ * HY * HX cells x chunks 16-byte units; every load of the
-        // thread is issued before the first store so they overlap
-        constexpr int UNITS = HZ * HY * HX * C::chunks;
-        constexpr int PER = (UNITS + THREADS - 1) / THREADS;
-        if (MODE == 0) {
-            float2 wv[PER];
-            float vv[PER], sv[PER];
-            bool ok[PER];
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int u = t + k * THREADS;
-                const int ch = u % C::chunks, cell = u / C::chunks;
-                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-                ok[k] = u < UNITS && ch == 0 && in_shell(g, x, y, z);
-                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-                wv[k] = ok[k] ? __ldg(Win + c) : make_float2(0.f, 0.f);
-                vv[k] = ok[k] ? __ldg(vel + c) : 0.f;
-                sv[k] = ok[k] ? __ldg(scal + c) : 1.f;
-            }
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int u = t + k * THREADS;
-                if (u >= UNITS) break;
-                const int ch = u % C::chunks, cell = u / C::chunks;
-                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (ok[k]) {
-                    const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-                    const float inv = 1.f / sv[k];
-                    v.x = pack2(wv[k].x * inv, wv[k].y * inv);
-                    v.y = pack2(vv[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
-                    v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
-                }
-                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v;
-            }
-        } else {
-            uint4 v[PER];
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int u = t + k * THREADS;
-                const int ch = u % C::chunks, cell = u / C::chunks;
-                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-                const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny), z = wrapi(z0 + hz - 1, g.nz);
-                const bool ok = u < UNITS && in_shell(g, x, y, z);
-                const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
-                v[k] = ok ? __ldg(reinterpret_cast<const uint4*>(act_in + c * CIN + ch * 8)) : make_uint4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int u = t + k * THREADS;
-                if (u >= UNITS) break;
-                const int ch = u % C::chunks, cell = u / C::chunks;
-                const int hx = cell % HX, hy = (cell / HX) % HY, hz = cell / (HX * HY);
-                *reinterpret_cast<uint4*>(sm + (((hz * HY + hy) * C::chunks + ch) * HX + hx) * 16) = v[k];
-            }
-        }
-        tc5::fence_async_smem();
-        tc5::fence_before_sync();
-        __syncthreads();
-        int bad = 0;
-        if (t == 0) {
-            tc5::fence_after_sync();
-            uint32_t acc = 0;
-            for (int tap = 0; tap < 27; ++tap) {
-                const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-                const uint32_t a0 = sbase + ((1 + dz) * HY + (1 + dy)) * C::sbo + (1 + dx) * 16;
-                const uint32_t b0 = sbase + C::off_w + tap * C::ngroups * C::chunks * 128;
-#pragma unroll
-                for (int k = 0; k < C::ksteps; ++k) {
-                    const uint64_t da = tc5::smem_desc(a0 + 2 * k * C::lbo, C::lbo, C::sbo);
-                    const uint64_t db = tc5::smem_desc(b0 + 2 * k * 128, 128, C::wsbo);
-                    tc5::mma_f16(tmem, da, db, C::id, acc);
-                    acc = 1;
-                }
-            }
-            tc5::mma_commit(bar);
-            bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
-        }
-        failed = __syncthreads_or(bad);
-        phase ^= 1u;
-        if (failed) break;
-        tc5::fence_after_sync();
-        const int x = x0 + (t & 7), y = y0 + (t >> 3), z = z0;
+    // outputs of plane z from the accumulator (after its MMAs completed)
+    auto epilogue = [&](int x0, int y0, int z) {
+        const int x = x0 + (t & 7), y = y0 + (t >> 3);
         const bool valid = x < g.nx && y < g.ny && in_shell(g, x, y, z);
         const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
         if (MODE == 2) {
@@ -236,12 +224,69 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
                 }
             }
         }
+    };
+
+    for (int col = blockIdx.x; col < ncols && !failed; col += gridDim.x) {
+        const int2 cd = cols[col];
+        const int x0 = (cd.x & 1023) * TXW, y0 = ((cd.x >> 10) & 1023) * TYW;
+        const int z0 = cd.y & 0xFFFF, len = cd.y >> 16;
+        // halo planes h = 0, 1 (z0 - 1, z0) into slots 0, 1
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const int z = wrapi(z0 + h - 1, g.nz);
+            load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, z, t);
+            store_plane<CIN, NPAD, MODE>(st, sm + h * C::plane_bytes, g, x0, y0, z, t);
+        }
+#pragma unroll 1
+        for (int k = 0; k < len; ++k) {
+            // halo plane h = k + 2 (z0 + k + 1) in flight while plane k - 1
+            // finishes
+            const int zh = wrapi(z0 + k + 1, g.nz);
+            load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, zh, t);
+            int bad = 0;
+            if (k > 0) {
+                bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
+                if (!bad) phase ^= 1u;
+                tc5::fence_after_sync();
+                if (!bad) epilogue(x0, y0, z0 + k - 1);
+            }
+            // the slot of plane k + 2 held plane k - 2, whose MMAs are done
+            store_plane<CIN, NPAD, MODE>(st, sm + ((k + 2) & (SLOTS - 1)) * C::plane_bytes, g, x0, y0, zh, t);
+            tc5::fence_async_smem();
+            tc5::fence_before_sync();
+            failed = __syncthreads_or(bad);
+            if (failed) break;
+            if (t == 0) {
+                tc5::fence_after_sync();
+                uint32_t acc = 0;
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+                    const uint32_t a0 = sbase + ((k + 1 + dz) & (SLOTS - 1)) * C::plane_bytes + (1 + dy) * C::sbo +
+                                        (1 + dx) * 16;
+                    const uint32_t b0 = sbase + C::off_w + tap * C::ngroups * C::chunks * 128;
+#pragma unroll
+                    for (int q = 0; q < C::ksteps; ++q) {
+                        const uint64_t da = tc5::smem_desc(a0 + 2 * q * C::lbo, C::lbo, C::sbo);
+                        const uint64_t db = tc5::smem_desc(b0 + 2 * q * 128, 128, C::wsbo);
+                        tc5::mma_f16(tmem, da, db, C::id, acc);
+                        acc = 1;
+                    }
+                }
+                tc5::mma_commit(bar);
+            }
+        }
+        if (failed) break;
+        // the column's last plane
+        int bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
+        if (!bad) phase ^= 1u;
+        tc5::fence_after_sync();
+        if (!bad) epilogue(x0, y0, z0 + len - 1);
         tc5::fence_before_sync();
-        __syncthreads();
+        failed = __syncthreads_or(bad);
     }
     if (failed && t == 0) {
         atomicExch(err, 2);
-        tc5::mbar_wait(bar, phase ^ 1u, kWaitLimitNs);
+        tc5::mbar_wait(bar, phase, kWaitLimitNs);
     }
     tc5::fence_before_sync();
     __syncthreads();
@@ -277,22 +322,32 @@ void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, 
             }
 }
 
-void tc_tiles(const NetGeom& g, std::vector<int>& tiles)
+// Columns of output planes: for each 8 x 16 (x, y) tile, the runs of
+// consecutive z planes holding shell cells, cut into pieces of at most ZL;
+// two ints per column (x tile | y tile << 10, z0 | planes << 16).
+void tc_tiles(const NetGeom& g, std::vector<int>& cols)
 {
-    tiles.clear();
+    cols.clear();
     const int tx = (g.nx + TXW - 1) / TXW, ty = (g.ny + TYW - 1) / TYW;
-    for (int z = 0; z < g.nz; ++z)
-        for (int j = 0; j < ty; ++j)
-            for (int i = 0; i < tx; ++i) {
+    for (int j = 0; j < ty; ++j)
+        for (int i = 0; i < tx; ++i) {
+            int run0 = -1;
+            for (int z = 0; z <= g.nz; ++z) {
                 bool any = false;
-                for (int y = j * TYW; y < std::min(g.ny, j * TYW + TYW) && !any; ++y)
+                for (int y = j * TYW; z < g.nz && y < std::min(g.ny, j * TYW + TYW) && !any; ++y)
                     for (int x = i * TXW; x < std::min(g.nx, i * TXW + TXW) && !any; ++x) {
                         const int d = std::min(std::min(std::min(x, g.nx - 1 - x), std::min(y, g.ny - 1 - y)),
                                                std::min(z, g.nz - 1 - z));
                         any = d < g.shell;
                     }
-                if (any) tiles.push_back(i | (j << 10) | (z << 20));
+                if (any && run0 < 0) run0 = z;
+                if ((!any || z - run0 == ZL) && run0 >= 0) {
+                    cols.push_back(i | (j << 10));
+                    cols.push_back(run0 | ((z - run0) << 16));
+                    run0 = any ? z : -1;
+                }
             }
+        }
 }
 
 cudaError_t configure_tc()
@@ -308,7 +363,7 @@ cudaError_t configure_tc()
                                 LayerCfg<32, 16>::smem);
 }
 
-cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel)
+cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W, const float* vel, bool scale)
 {
     static int sms = 0;
     if (!sms) {
@@ -318,16 +373,17 @@ cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W,
         if (sms <= 0) sms = 148;
     }
     const unsigned grid = (unsigned)std::max(1, std::min(tc.ntiles, 2 * sms));
-    cudaError_t e = shell_scale(s, n, W);
+    const int2* cols = reinterpret_cast<const int2*>(tc.tiles);
+    cudaError_t e = scale ? shell_scale(s, n, W) : cudaSuccess;
     if (e != cudaSuccess) return e;
     k_conv_tc<16, 32, 0><<<grid, THREADS, LayerCfg<16, 32>::smem, s>>>(
-        nullptr, W, vel, tc.w[0], tc.b[0], tc.act[0], nullptr, n.sloc, n.g, tc.tiles, tc.ntiles, tc.err);
+        nullptr, W, vel, tc.w[0], tc.b[0], tc.act[0], nullptr, n.sloc, n.g, cols, tc.ntiles, tc.err);
     k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
-        tc.act[0], nullptr, nullptr, tc.w[1], tc.b[1], tc.act[1], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+        tc.act[0], nullptr, nullptr, tc.w[1], tc.b[1], tc.act[1], nullptr, n.scal, n.g, cols, tc.ntiles, tc.err);
     k_conv_tc<32, 32, 1><<<grid, THREADS, LayerCfg<32, 32>::smem, s>>>(
-        tc.act[1], nullptr, nullptr, tc.w[2], tc.b[2], tc.act[0], nullptr, n.scal, n.g, tc.tiles, tc.ntiles, tc.err);
+        tc.act[1], nullptr, nullptr, tc.w[2], tc.b[2], tc.act[0], nullptr, n.scal, n.g, cols, tc.ntiles, tc.err);
     k_conv_tc<32, 16, 2><<<grid, THREADS, LayerCfg<32, 16>::smem, s>>>(
-        tc.act[0], nullptr, nullptr, tc.w[3], tc.b[3], nullptr, W, n.sloc, n.g, tc.tiles, tc.ntiles, tc.err);
+        tc.act[0], nullptr, nullptr, tc.w[3], tc.b[3], nullptr, W, n.sloc, n.g, cols, tc.ntiles, tc.err);
     return cudaGetLastError();
 }
 
