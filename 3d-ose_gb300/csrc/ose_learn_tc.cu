@@ -3,17 +3,19 @@
 // and activations and an FP32 accumulator in TMEM.
 //
 // A CTA walks a column of output planes: 8 (x) x 16 (y) cells, the M rows of
-// the MMA (row m = y * 8 + x), for up to ZL consecutive z.  The input halo
-// planes (10 x 18 cells, all input channels) sit in a ring of four shared-
+// the MMA (row m = y * 8 + x), for up to ZL consecutive z.  It streams the
+// input halo planes (10 x 18 cells, all input channels) through two shared-
 // memory slots, each in the layout [y 18][channel chunk][x 10][8 channels x
-// 2 bytes]: for a tap (dx, dy, dz) the 128 x Cin operand is a plain K-major
-// descriptor into the slot of plane z + dz (rows 16 bytes apart, y groups SBO
-// apart, channel chunks LBO apart, start shifted by dx * 16 bytes), so no
-// im2col copy is made.  An output plane is 27 taps x Cin / 16 MMAs of
-// 128 x N x 16 (N = 32, or 16 for the 2-channel output layer padded with zero
-// weights), accumulated in TMEM.  Moving one plane along z loads one new halo
-// plane (180 cells for 128 outputs), and its global loads are in flight while
-// the CTA waits for the previous plane's MMAs and writes its outputs.
+// 2 bytes]: for an in-plane tap (dx, dy) the 128 x Cin operand is a plain
+// K-major descriptor into the slot (rows 16 bytes apart, y groups SBO apart,
+// channel chunks LBO apart, start shifted by dx * 16 bytes), so no im2col
+// copy is made.  A halo plane at z feeds the outputs at z + 1, z and z - 1
+// (taps dz = -1, 0, +1), so the B operand of a tap (dx, dy) holds the three
+// dz weight blocks side by side and one MMA of N = 3 Cout updates the three
+// output planes' accumulators, which sit next to one another in a ring of
+// eight accumulators in TMEM: each halo plane is read by the tensor core 9
+// times instead of 27.  The global loads of the next halo plane are in flight
+// while the CTA writes out the plane that the last MMAs completed.
 //
 // Layer 0's halo is built from the state and the velocity (the 8 features,
 // padded to 16 channels with zeros); hidden activations are BF16 [cell][32];
@@ -39,8 +41,12 @@ namespace {
 constexpr int TXW = 8, TYW = 16;              // output tile (x, y) of one z plane
 constexpr int HX = TXW + 2, HY = TYW + 2;
 constexpr int ZL = 16;                        // output planes per column at most
-constexpr int SLOTS = 4;                      // ring of halo planes
-constexpr int THREADS = 128;                  // one output row (cell) per thread
+constexpr int SLOTS = 2;                      // halo plane slots per pipeline
+constexpr int RING = 4;                       // accumulators (output planes) per pipeline in TMEM
+constexpr int kMinSmem = 80 * 1024;           // at most two CTAs per SM (their TMEM)
+constexpr int PIPE_THREADS = 128;             // one output row (cell) per thread
+constexpr int PIPES = 2;                      // independent columns per CTA (shared weights)
+constexpr int THREADS = PIPES * PIPE_THREADS;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -77,22 +83,24 @@ template <int CIN, int NPAD>
 struct LayerCfg {
     static constexpr int chunks = CIN / 8;                       // 16-byte channel chunks
     static constexpr int plane_bytes = HY * chunks * HX * 16;    // one halo plane
-    static constexpr int halo_bytes = SLOTS * plane_bytes;
+    static constexpr int halo_bytes = PIPES * SLOTS * plane_bytes;
     static constexpr uint32_t lbo = HX * 16;                     // chunk stride in a plane
     static constexpr uint32_t sbo = chunks * HX * 16;            // y stride in a plane
-    static constexpr int ngroups = NPAD / 8;
-    static constexpr int w_bytes = 27 * ngroups * chunks * 128;  // B operands, all taps
+    static constexpr int ngroups = 3 * NPAD / 8;                 // B rows: dz = +1, 0, -1 blocks
+    static constexpr int tap_bytes = ngroups * chunks * 128;     // B operand of one (dx, dy)
+    static constexpr int w_bytes = 9 * tap_bytes;
     static constexpr uint32_t wsbo = chunks * 128;               // B: n-group stride
     static constexpr int ksteps = CIN / 16;
     static constexpr int off_w = halo_bytes;
     static constexpr int off_bias = off_w + w_bytes;
-    static constexpr int off_bar = off_bias + NPAD * 4;
-    static constexpr int smem = off_bar + 16;
-    static constexpr uint32_t id = tc5::idesc(tc5::kTypeBF16, 128, NPAD);
+    static constexpr int off_bar = off_bias + NPAD * 4;          // 2 mbarriers per pipeline, TMEM address
+    static constexpr int used = off_bar + 8 * 2 * PIPES + 8;
+    static constexpr int smem = used > kMinSmem ? used : kMinSmem;
+    static constexpr int tmem_cols = PIPES * RING * NPAD;
     // staged loads of one halo plane per thread: cells (layer 0) or 16-byte units
     static constexpr int cells = HY * HX;
     static constexpr int units = cells * chunks;
-    static constexpr int per = ((CIN == 16 ? cells : units) + THREADS - 1) / THREADS;
+    static constexpr int per = ((CIN == 16 ? cells : units) + PIPE_THREADS - 1) / PIPE_THREADS;
 };
 
 // One halo plane in registers: layer 0 keeps the state, velocity and scale of
@@ -113,7 +121,7 @@ __device__ __forceinline__ void load_plane(Staged<MODE, LayerCfg<CIN, NPAD>::per
     using C = LayerCfg<CIN, NPAD>;
 #pragma unroll
     for (int k = 0; k < C::per; ++k) {
-        const int u = t + k * THREADS;
+        const int u = t + k * PIPE_THREADS;
         const int ch = MODE == 0 ? 0 : u % C::chunks, cell = MODE == 0 ? u : u / C::chunks;
         const int hx = cell % HX, hy = cell / HX;
         const int x = wrapi(x0 + hx - 1, g.nx), y = wrapi(y0 + hy - 1, g.ny);
@@ -137,7 +145,7 @@ __device__ __forceinline__ void store_plane(const Staged<MODE, LayerCfg<CIN, NPA
     using C = LayerCfg<CIN, NPAD>;
 #pragma unroll
     for (int k = 0; k < C::per; ++k) {
-        const int u = t + k * THREADS;
+        const int u = t + k * PIPE_THREADS;
         if (u >= (MODE == 0 ? C::cells : C::units)) break;
         const int ch = MODE == 0 ? 0 : u % C::chunks, cell = MODE == 0 ? u : u / C::chunks;
         const int hx = cell % HX, hy = cell / HX;
@@ -155,29 +163,59 @@ __device__ __forceinline__ void store_plane(const Staged<MODE, LayerCfg<CIN, NPA
     }
 }
 
+// Barrier of one pipeline's 128 threads (named barrier 1 + pipe); returns
+// whether any of them passed v != 0.
+__device__ __forceinline__ int pipe_sync_or(int pipe, int v)
+{
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(v), "r"(1 + pipe), "n"(PIPE_THREADS)
+        : "memory");
+    return r;
+}
+
 // MODE 0: layer 0 (features from state + velocity), hidden output (ReLU, BF16)
 // MODE 1: hidden layer, BF16 in, hidden output
 // MODE 2: output layer, BF16 in, state += s(x) (o0, o1) at the write cells
 // (scal = the local scale s(x) per cell).  cols: (x tile | y tile << 10,
 // z0 | planes << 16) per column.
+//
+// The CTA runs two independent pipelines (threads 0-127 and 128-255), each
+// with its own halo slots, mbarriers and TMEM accumulators, over alternate
+// columns; the weights in shared memory serve both.  Halo plane p of a
+// column (p = 0 .. len + 1, z = z0 - 1 + p) feeds outputs q = p - 2
+// (dz = +1), p - 1 (dz = 0) and p (dz = -1), q in [0, len); output q is
+// complete after plane q + 2.  Iteration p: barrier (plane p in slot p & 1),
+// MMAs of plane p, loads of plane p + 1, wait for the MMAs of plane p - 1,
+// write output p - 3, store plane p + 1 into the slot plane p - 1 left.
 template <int CIN, int NPAD, int MODE>
-__global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict__ act_in,
-                                                     const float2* __restrict__ Win, const float* __restrict__ vel,
-                                                     const uint8_t* __restrict__ wts, const float* __restrict__ bias,
-                                                     uint16_t* __restrict__ act_out, float2* __restrict__ state,
-                                                     const float* __restrict__ scal, NetGeom g,
-                                                     const int2* __restrict__ cols, int ncols, int* err)
+__global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restrict__ act_in,
+                                                        const float2* __restrict__ Win, const float* __restrict__ vel,
+                                                        const uint8_t* __restrict__ wts, const float* __restrict__ bias,
+                                                        uint16_t* __restrict__ act_out, float2* __restrict__ state,
+                                                        const float* __restrict__ scal, NetGeom g,
+                                                        const int2* __restrict__ cols, int ncols, int* err)
 {
     using C = LayerCfg<CIN, NPAD>;
     extern __shared__ __align__(1024) uint8_t sm[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::off_bar);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::off_bar + 8);
+    const int t = threadIdx.x, warp = t >> 5, pipe = t / PIPE_THREADS, tl = t % PIPE_THREADS;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::off_bar) + 2 * pipe;   // this pipeline's two
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::off_bar + 16 * PIPES);
     float* sb = reinterpret_cast<float*>(sm + C::off_bias);
-    const uint32_t sbase = tc5::smem_u32(sm);
-    const int t = threadIdx.x, warp = t >> 5;
+    uint8_t* halo = sm + pipe * SLOTS * C::plane_bytes;
+    const uint32_t hbase = tc5::smem_u32(halo);
+    const uint32_t wbase = tc5::smem_u32(sm + C::off_w);
 
-    if (warp == 0) tc5::tmem_alloc(tslot, 32);
-    if (t == 0) tc5::mbar_init(bar, 1);
+    if (warp == 0) tc5::tmem_alloc(tslot, C::tmem_cols);
+    if (tl == 0) {
+        tc5::mbar_init(bar, 1);
+        tc5::mbar_init(bar + 1, 1);
+    }
     {
         const int4* s4 = reinterpret_cast<const int4*>(wts);
         int4* d4 = reinterpret_cast<int4*>(sm + C::off_w);
@@ -187,20 +225,21 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
     tc5::fence_before_sync();
     __syncthreads();
     tc5::fence_after_sync();
-    const uint32_t tmem = *tslot;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tmem = *tslot + (uint32_t)(pipe * RING * NPAD);
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     int failed = 0;
-    uint32_t phase = 0;
+    uint32_t ph = 0u;   // bit b: the parity to wait for on bar[b]
     Staged<MODE, C::per> st;
 
-    // outputs of plane z from the accumulator (after its MMAs completed)
-    auto epilogue = [&](int x0, int y0, int z) {
-        const int x = x0 + (t & 7), y = y0 + (t >> 3);
+    // outputs of plane z from accumulator `slot` (after its MMAs completed)
+    auto epilogue = [&](int x0, int y0, int z, int slot) {
+        const int x = x0 + (tl & 7), y = y0 + (tl >> 3);
         const bool valid = x < g.nx && y < g.ny && in_shell(g, x, y, z);
         const size_t c = ((size_t)z * g.ny + y) * g.nx + x;
+        const uint32_t ta = trow + (uint32_t)(slot * NPAD);
         if (MODE == 2) {
             float o[16];
-            tc5::tmem_ld16(trow, o);
+            tc5::tmem_ld16(ta, o);
             if (valid && is_write(g, x, y, z)) {
                 const float sc = scal[c];
                 float2 w = state[c];
@@ -210,7 +249,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
             }
         } else {
             float o[32];
-            tc5::tmem_ld32(trow, o);
+            tc5::tmem_ld32(ta, o);
             if (valid) {
                 uint4* dst = reinterpret_cast<uint4*>(act_out + c * 32);
 #pragma unroll
@@ -226,73 +265,91 @@ __global__ void __launch_bounds__(THREADS) k_conv_tc(const uint16_t* __restrict_
         }
     };
 
-    for (int col = blockIdx.x; col < ncols && !failed; col += gridDim.x) {
+    // MMAs of one (dx, dy, k step) of halo plane p into the accumulators of
+    // outputs qa..qb (contiguous ring runs; B rows of output q start at block
+    // q - (p - 2))
+    auto issue = [&](int p, int qa, int qb, uint64_t da, uint32_t b0, uint32_t acc) {
+        while (qa <= qb) {
+            const int s = qa & (RING - 1);
+            const int cnt = min(qb - qa + 1, RING - s);
+            const int blk = qa - (p - 2);
+            const uint64_t db = tc5::smem_desc(b0 + blk * (NPAD / 8) * C::wsbo, 128, C::wsbo);
+            tc5::mma_f16(tmem + (uint32_t)(s * NPAD), da, db, tc5::idesc(tc5::kTypeBF16, 128, cnt * NPAD), acc);
+            qa += cnt;
+        }
+    };
+
+    for (int col = blockIdx.x * PIPES + pipe; col < ncols && !failed; col += gridDim.x * PIPES) {
         const int2 cd = cols[col];
         const int x0 = (cd.x & 1023) * TXW, y0 = ((cd.x >> 10) & 1023) * TYW;
         const int z0 = cd.y & 0xFFFF, len = cd.y >> 16;
-        // halo planes h = 0, 1 (z0 - 1, z0) into slots 0, 1
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            const int z = wrapi(z0 + h - 1, g.nz);
-            load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, z, t);
-            store_plane<CIN, NPAD, MODE>(st, sm + h * C::plane_bytes, g, x0, y0, z, t);
+        {
+            const int z = wrapi(z0 - 1, g.nz);
+            load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, z, tl);
+            store_plane<CIN, NPAD, MODE>(st, halo, g, x0, y0, z, tl);
         }
+        int bad = 0;
 #pragma unroll 1
-        for (int k = 0; k < len; ++k) {
-            // halo plane h = k + 2 (z0 + k + 1) in flight while plane k - 1
-            // finishes
-            const int zh = wrapi(z0 + k + 1, g.nz);
-            load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, zh, t);
-            int bad = 0;
-            if (k > 0) {
-                bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
-                if (!bad) phase ^= 1u;
-                tc5::fence_after_sync();
-                if (!bad) epilogue(x0, y0, z0 + k - 1);
-            }
-            // the slot of plane k + 2 held plane k - 2, whose MMAs are done
-            store_plane<CIN, NPAD, MODE>(st, sm + ((k + 2) & (SLOTS - 1)) * C::plane_bytes, g, x0, y0, zh, t);
+        for (int p = 0; p <= len + 1; ++p) {
             tc5::fence_async_smem();
             tc5::fence_before_sync();
-            failed = __syncthreads_or(bad);
+            failed = pipe_sync_or(pipe, bad);
             if (failed) break;
-            if (t == 0) {
+            if (tl == 0) {
                 tc5::fence_after_sync();
-                uint32_t acc = 0;
-                for (int tap = 0; tap < 27; ++tap) {
-                    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-                    const uint32_t a0 = sbase + ((k + 1 + dz) & (SLOTS - 1)) * C::plane_bytes + (1 + dy) * C::sbo +
-                                        (1 + dx) * 16;
-                    const uint32_t b0 = sbase + C::off_w + tap * C::ngroups * C::chunks * 128;
+                const int qa = max(p - 2, 0), qb = min(p, len - 1);
+                const bool fresh = p <= len - 1;   // output p starts here
+                const uint32_t slot = hbase + (p & 1) * C::plane_bytes;
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int dx = tap % 3 - 1, dy = tap / 3 - 1;
+                    const uint32_t a0 = slot + (1 + dy) * C::sbo + (1 + dx) * 16;
+                    const uint32_t b0 = wbase + tap * C::tap_bytes;
 #pragma unroll
-                    for (int q = 0; q < C::ksteps; ++q) {
-                        const uint64_t da = tc5::smem_desc(a0 + 2 * q * C::lbo, C::lbo, C::sbo);
-                        const uint64_t db = tc5::smem_desc(b0 + 2 * q * 128, 128, C::wsbo);
-                        tc5::mma_f16(tmem, da, db, C::id, acc);
-                        acc = 1;
+                    for (int k = 0; k < C::ksteps; ++k) {
+                        const uint64_t da = tc5::smem_desc(a0 + 2 * k * C::lbo, C::lbo, C::sbo);
+                        if (fresh && tap == 0 && k == 0) {
+                            issue(p, qa, p - 1, da, b0 + 2 * k * 128, 1u);
+                            issue(p, p, p, da, b0 + 2 * k * 128, 0u);
+                        } else {
+                            issue(p, qa, qb, da, b0 + 2 * k * 128, 1u);
+                        }
                     }
                 }
-                tc5::mma_commit(bar);
+                tc5::mma_commit(bar + (p & 1));
             }
+            const int zn = wrapi(z0 + p, g.nz);   // halo plane p + 1
+            if (p <= len) load_plane<CIN, NPAD, MODE>(st, act_in, Win, vel, scal, g, x0, y0, zn, tl);
+            if (p >= 1) {
+                const int b = (p - 1) & 1;
+                bad = !tc5::mbar_wait(bar + b, (ph >> b) & 1u, kWaitLimitNs);
+                if (!bad) ph ^= 1u << b;
+                tc5::fence_after_sync();
+                if (!bad && p >= 3) epilogue(x0, y0, z0 + p - 3, (p - 3) & (RING - 1));
+            }
+            if (p <= len) store_plane<CIN, NPAD, MODE>(st, halo + ((p + 1) & 1) * C::plane_bytes, g, x0, y0, zn, tl);
         }
         if (failed) break;
-        // the column's last plane
-        int bad = !tc5::mbar_wait(bar, phase, kWaitLimitNs);
-        if (!bad) phase ^= 1u;
-        tc5::fence_after_sync();
-        if (!bad) epilogue(x0, y0, z0 + len - 1);
+        // the column's last plane, after the MMAs of halo plane len + 1
+        {
+            const int b = (len + 1) & 1;
+            bad = !tc5::mbar_wait(bar + b, (ph >> b) & 1u, kWaitLimitNs);
+            if (!bad) ph ^= 1u << b;
+            tc5::fence_after_sync();
+            if (!bad) epilogue(x0, y0, z0 + len - 1, (len - 1) & (RING - 1));
+        }
         tc5::fence_before_sync();
-        failed = __syncthreads_or(bad);
+        failed = pipe_sync_or(pipe, bad);
     }
-    if (failed && t == 0) {
+    if (failed && tl == 0) {
         atomicExch(err, 2);
-        tc5::mbar_wait(bar, phase, kWaitLimitNs);
+        tc5::mbar_wait(bar, ph & 1u, kWaitLimitNs);
+        tc5::mbar_wait(bar + 1, (ph >> 1) & 1u, kWaitLimitNs);
     }
     tc5::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
         tc5::fence_after_sync();
-        tc5::tmem_dealloc(tmem, 32);
+        tc5::tmem_dealloc(*tslot, C::tmem_cols);
     }
 }
 
@@ -307,17 +364,21 @@ uint16_t bf16_bits(float f)
 }  // namespace
 
 // Host: BF16 B operands of one layer in the kernel's shared-memory layout
-// [tap][n group][channel chunk][8 rows][8 channels], zero beyond (cin, cout).
+// [dx, dy][n group][channel chunk][8 rows][8 channels], row n = blk * npad +
+// output channel with blk 0, 1, 2 the taps dz = +1, 0, -1; zero beyond
+// (cin, cout).  w: [tap = (dz + 1) 9 + (dy + 1) 3 + dx + 1][cin][cout].
 void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, std::vector<uint8_t>& out)
 {
-    const int chunks = cin_pad / 8, ngroups = npad / 8;
-    out.assign((size_t)27 * ngroups * chunks * 128, 0);
-    for (int tap = 0; tap < 27; ++tap)
-        for (int n = 0; n < npad; ++n)
+    const int chunks = cin_pad / 8, ngroups = 3 * npad / 8;
+    out.assign((size_t)9 * ngroups * chunks * 128, 0);
+    for (int dxy = 0; dxy < 9; ++dxy)
+        for (int n = 0; n < 3 * npad; ++n)
             for (int k = 0; k < cin_pad; ++k) {
-                const float v = (n < cout && k < cin) ? w[((size_t)tap * cin + k) * cout + n] : 0.f;
+                const int blk = n / npad, co = n % npad, dz = 1 - blk;
+                const int tap = (dz + 1) * 9 + dxy;
+                const float v = (co < cout && k < cin) ? w[((size_t)tap * cin + k) * cout + co] : 0.f;
                 const uint16_t b = bf16_bits(v);
-                const size_t o = (((size_t)tap * ngroups + n / 8) * chunks + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+                const size_t o = (((size_t)dxy * ngroups + n / 8) * chunks + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
                 memcpy(out.data() + o, &b, 2);
             }
 }
@@ -372,7 +433,7 @@ cudaError_t forward_tc(cudaStream_t s, const Net& n, const TcNet& tc, float2* W,
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    const unsigned grid = (unsigned)std::max(1, std::min(tc.ntiles, 2 * sms));
+    const unsigned grid = (unsigned)std::max(1, std::min((tc.ntiles + PIPES - 1) / PIPES, 2 * sms));
     const int2* cols = reinterpret_cast<const int2*>(tc.tiles);
     cudaError_t e = scale ? shell_scale(s, n, W) : cudaSuccess;
     if (e != cudaSuccess) return e;

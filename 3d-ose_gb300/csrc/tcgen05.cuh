@@ -42,7 +42,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 // Instruction descriptor of kind::tf32 / kind::f16: D F32 (bits 4-5 = 1),
 // A/B type (bits 7-9, 10-12: 2 = TF32, 1 = BF16), both K-major, N >> 3 at
 // bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t idesc(uint32_t ab_type, int M, int N)
+__host__ __device__ constexpr uint32_t idesc(uint32_t ab_type, int M, int N)
 {
     return (1u << 4) | (ab_type << 7) | (ab_type << 10) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(M >> 4) << 24);
@@ -91,8 +91,8 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
 {
     const uint32_t a = smem_u32(bar);
-    const uint64_t t0 = global_ns();
-    for (;;) {
+    uint64_t t0 = 0;
+    for (bool first = true;; first = false) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -102,7 +102,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if (global_ns() - t0 > limit_ns) return false;
+        if (first) t0 = global_ns();   // the timer is read only once a wait is needed
+        else if (global_ns() - t0 > limit_ns) return false;
     }
 }
 
