@@ -74,34 +74,6 @@ __device__ __forceinline__ void tile_origin(int tp, int& x0, int& y0, int& z0)
     z0 = (tp >> 20) * T;
 }
 
-// Sum of P^2 + Q^2 over the shell -> acc[0] (atomic, zeroed by the caller).
-__global__ void k_shell_sumsq(const float2* __restrict__ W, NetGeom g, const int* __restrict__ tiles, int ntiles,
-                              float* acc)
-{
-    float s = 0.f;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        int x0, y0, z0;
-        tile_origin(tiles[tile], x0, y0, z0);
-        for (int t = threadIdx.x; t < T * T * T; t += blockDim.x) {
-            const int x = x0 + (t & 7), y = y0 + ((t >> 3) & 7), z = z0 + (t >> 6);
-            if (x < g.nx && y < g.ny && z < g.nz && in_shell(g, x, y, z)) {
-                const float2 w = W[((size_t)z * g.ny + y) * g.nx + x];
-                s = fmaf(w.x, w.x, fmaf(w.y, w.y, s));
-            }
-        }
-    }
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
-}
-
-// scal[1] = s = sqrt(acc / (2 n)), scal[2] = 1/s (0 for a zero field).
-__global__ void k_shell_scale(float* scal, float inv_count2)
-{
-    const float s = sqrtf(scal[0] * inv_count2);
-    scal[1] = s;
-    scal[2] = s > 0.f ? 1.f / s : 0.f;
-}
-
 // Local scale s(x): three periodic box sums of P^2 + Q^2 (shell cells) with
 // half-width kBoxR, x then y then z over the whole padded grid.  Each pass
 // stages whole lines in shared memory (coalesced global reads and writes)
@@ -109,27 +81,77 @@ __global__ void k_shell_scale(float* scal, float inv_count2)
 constexpr int kBoxR = 8;
 constexpr int kBoxTX = 32;   // x columns per block of the y and z passes
 
-__device__ __forceinline__ int modi(int v, int n) { return ((v % n) + n) % n; }
-
-// block per (y, z) row; e[x] with its periodic halo in shared memory
-__global__ void k_box_x(const float2* __restrict__ W, float* __restrict__ out, NetGeom g)
+// rows of the x pass per block (shared memory <= 48 KiB)
+static int box_rows(const NetGeom& g) { return std::max(1, std::min(8, 12288 / (g.nx + 2 * kBoxR))); }
+static int box_blocks(const NetGeom& g)
 {
-    extern __shared__ float box_e[];   // [nx + 2 kBoxR]
-    const int row = blockIdx.x, y = row % g.ny, z = row / g.ny;
-    const float2* w = W + (size_t)row * g.nx;
-    for (int j = threadIdx.x; j < g.nx + 2 * kBoxR; j += blockDim.x) {
-        const int x = modi(j - kBoxR, g.nx);
-        const float2 v = w[x];
-        box_e[j] = in_shell(g, x, y, z) ? fmaf(v.x, v.x, v.y * v.y) : 0.f;
+    const int r = box_rows(g);
+    return (g.ny * g.nz + r - 1) / r;
+}
+
+// x pass over `rows` (y, z) rows per block, e[x] with its periodic halo in
+// shared memory; also the block's sum of e over its rows -> part[block].
+__global__ void __launch_bounds__(256) k_box_x(const float2* __restrict__ W, float* __restrict__ out,
+                                               float* __restrict__ part, NetGeom g, int rows)
+{
+    extern __shared__ float box_e[];   // [rows][nx + 2 kBoxR]
+    __shared__ float red[8];
+    const int L = g.nx + 2 * kBoxR;
+    const int row0 = blockIdx.x * rows, nr = min(rows, g.ny * g.nz - row0);
+    float sum = 0.f;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
+        const int r = i / L, j = i - r * L;
+        const int row = row0 + r, y = row % g.ny, z = row / g.ny;
+        const int x = wrapi(j - kBoxR, g.nx);
+        const float2 v = W[(size_t)row * g.nx + x];
+        const float e = in_shell(g, x, y, z) ? fmaf(v.x, v.x, v.y * v.y) : 0.f;
+        box_e[i] = e;
+        if (j >= kBoxR && j < g.nx + kBoxR) sum += e;
     }
     __syncthreads();
-    float* o = out + (size_t)row * g.nx;
-    for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+    for (int i = threadIdx.x; i < nr * g.nx; i += blockDim.x) {
+        const int r = i / g.nx, x = i - r * g.nx;
+        const float* e = box_e + r * L + x;
         float acc = 0.f;
-        for (int d = 0; d <= 2 * kBoxR; ++d) acc += box_e[x + d];
-        o[x] = acc;
+#pragma unroll
+        for (int d = 0; d <= 2 * kBoxR; ++d) acc += e[d];
+        out[(size_t)(row0 + r) * g.nx + x] = acc;
+    }
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+        part[blockIdx.x] = b;
     }
 }
+
+// scal[0] = sum of P^2 + Q^2 over the shell (the x pass's block sums, added
+// in a fixed order), scal[1] = s = sqrt(scal[0] / (2 n)), scal[2] = 1/s (0 for
+// a zero field).
+__global__ void __launch_bounds__(1024) k_shell_scale(float* scal, const float* __restrict__ part, int nparts,
+                                                      float inv_count2)
+{
+    __shared__ double red[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) a += part[i];
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        const float sum = (float)t;
+        const float s = sqrtf(sum * inv_count2);
+        scal[0] = sum;
+        scal[1] = s;
+        scal[2] = s > 0.f ? 1.f / s : 0.f;
+    }
+}
+
+__device__ __forceinline__ int modi(int v, int n) { return ((v % n) + n) % n; }
 
 // block per (x tile, plane index, chunk of kBoxL outputs): lines of length n
 // at stride `stride` (y pass: n = ny, stride nx, plane = z; z pass: n = nz,
@@ -501,14 +523,13 @@ static unsigned grid_for(int ntiles, int per_sm)
 
 cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
 {
-    cudaMemsetAsync(n.scal, 0, sizeof(float), s);
-    const unsigned gr = grid_for(n.ntiles, 2);
-    k_shell_sumsq<<<gr, 256, 0, s>>>(W, n.g, n.tiles, n.ntiles, n.scal);
-    k_shell_scale<<<1, 1, 0, s>>>(n.scal, (float)(0.5 / (double)std::max(1LL, n.ncells)));
     const NetGeom& g = n.g;
     const long long plane = (long long)g.nx * g.ny;
     const unsigned xt = (unsigned)((g.nx + kBoxTX - 1) / kBoxTX);
-    k_box_x<<<g.ny * g.nz, 256, sizeof(float) * (g.nx + 2 * kBoxR), s>>>(W, n.sloc, g);
+    const int rows = box_rows(g), nb = box_blocks(g);
+    float* part = n.scal + 4;
+    k_box_x<<<nb, 256, sizeof(float) * rows * (g.nx + 2 * kBoxR), s>>>(W, n.sloc, part, g, rows);
+    k_shell_scale<<<1, 1024, 0, s>>>(n.scal, part, nb, (float)(0.5 / (double)std::max(1LL, n.ncells)));
     k_box_lines<false><<<dim3(xt, g.nz, (g.ny + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
         n.sloc, n.stmp, n.scal, g.ny, g.nx, plane, g.nx);
     k_box_lines<true><<<dim3(xt, g.ny, (g.nz + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
@@ -653,7 +674,7 @@ cudaError_t create_net(ose_corrector* c, const NetGeom& g, bool training, bool f
     if ((e = cudaMemcpy(n.tiles, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
         return e;
     A_(n.params, np);
-    A_(n.scal, 4);
+    A_(n.scal, 4 + (size_t)box_blocks(g));   // + the x pass's block sums
     A_(n.loss, 1);
     A_(n.sloc, cells);
     A_(n.stmp, cells);
