@@ -38,7 +38,12 @@ constexpr int N = 256;          // line length on all three axes
 constexpr bool kCompensatedTwiddles = false;
 constexpr int CL = 8;           // CTAs per cluster (one plane per cluster)
 constexpr int SL = N / CL;      // rows / columns per CTA = 32
-constexpr int THREADS = 256;
+// Line slots per thread: 2 (256 threads, up to 128 registers) or 1 (512
+// threads, up to 64 registers); either way two CTAs per SM.
+constexpr int NS = 2;
+constexpr int THREADS = 512 / NS;
+constexpr int WARPS = THREADS / 32;
+constexpr int ECH = NS == 1 ? 4 : 8;   // epilogue cells loaded ahead of their stores
 constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
@@ -142,22 +147,22 @@ __device__ __forceinline__ void dft16(float2 (&v)[16])
 }
 
 // Rows context (x transforms): slot s of thread t handles row
-// (warp + 8 s) * 2 + lane / 16 and line thread j = lane % 16.
+// (warp + WARPS s) * 2 + lane / 16 and line thread j = lane % 16.
 struct RowSlot {
     int row, j;
 };
 __device__ __forceinline__ RowSlot row_slot(int s)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    return {(warp + 8 * s) * 2 + (lane >> 4), lane & 15};
+    return {(warp + WARPS * s) * 2 + (lane >> 4), lane & 15};
 }
-// Columns context (y and z transforms): column c = lane, line thread j = warp + 8 s.
+// Columns context (y and z transforms): column c = lane, line thread j = warp + WARPS s.
 struct ColSlot {
     int c, j;
 };
 __device__ __forceinline__ ColSlot col_slot(int s)
 {
-    return {(int)(threadIdx.x & 31), (int)(threadIdx.x >> 5) + 8 * s};
+    return {(int)(threadIdx.x & 31), (int)(threadIdx.x >> 5) + WARPS * s};
 }
 
 // Exchange between the two radix-16 stages for both slots of every thread.
@@ -166,7 +171,7 @@ template <bool ROWS>
 __device__ __forceinline__ void exchange(float2* T, float2 (&v0)[16], float2 (&v1)[16])
 {
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         float2(&v)[16] = s ? v1 : v0;
         if (ROWS) {
             const RowSlot q = row_slot(s);
@@ -181,7 +186,7 @@ __device__ __forceinline__ void exchange(float2* T, float2 (&v0)[16], float2 (&v
     }
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         float2(&v)[16] = s ? v1 : v0;
         if (ROWS) {
             const RowSlot q = row_slot(s);
@@ -203,7 +208,7 @@ template <bool INV, bool ROWS>
 __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)[16], float2 (&v1)[16])
 {
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         float2(&v)[16] = s ? v1 : v0;
         const int j = ROWS ? row_slot(s).j : col_slot(s).j;
         dft16<INV>(v);
@@ -212,7 +217,7 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
     }
     exchange<ROWS>(T, v0, v1);
     dft16<INV>(v0);
-    dft16<INV>(v1);
+    if (NS > 1) dft16<INV>(v1);
 }
 
 struct Args {
@@ -252,7 +257,7 @@ __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* s
     // natural-order rows into this CTA's slice A[row][kx]
     float2* A = smem;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const RowSlot q = row_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -261,7 +266,7 @@ __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* s
     cluster.sync();
     // columns 32r..32r+31 of all 256 rows from the 8 slices
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -274,7 +279,7 @@ __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* s
     fft256<false, false>(T, tw, v0, v1);
     float2* out = dst + (size_t)z * N * N + SL * r;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -294,7 +299,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     float2 v0[16], v1[16];
     const float2* in = a.src + ((size_t)z * N + SL * r) * N;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const RowSlot q = row_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -307,7 +312,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
 // recurrence, add_bessel_3d and apply_ABC_Xt of ose_3d_lib.cu:651-870, fused.
 // v holds the unnormalised inverse transform on entry and the new term a_{n+1}
-// (FIRST: a_1) on exit.  Loads are issued 8 cells at a time ahead of any
+// (FIRST: a_1) on exit.  Loads are issued ECH cells at a time ahead of any
 // store; the buffers never overlap at different cells, so the restrict
 // qualifiers are exact.
 template <int EPI>
@@ -321,12 +326,12 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
     const size_t rowbase = ((size_t)z * N + y) * N + j;
     const float attyz = (EPI == EPI_FIRST || EPI == EPI_SCALE) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float vv[8];
-        float2 am[8], sm[8];
+    for (int h = 0; h < 16 / ECH; ++h) {
+        float vv[ECH];
+        float2 am[ECH], sm[ECH];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const size_t i = rowbase + 16 * (8 * h + q);
+        for (int q = 0; q < ECH; ++q) {
+            const size_t i = rowbase + 16 * (ECH * h + q);
             vv[q] = __ldg(vs + i);
             if (EPI == EPI_FIRST) am[q] = w[i];
             if (EPI == EPI_MID || EPI == EPI_LAST) {
@@ -335,8 +340,8 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
             }
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int n1 = 8 * h + q;
+        for (int q = 0; q < ECH; ++q) {
+            const int n1 = ECH * h + q;
             const int x = 16 * n1 + j;
             const size_t i = rowbase + 16 * n1;
             // L a_n = v * X * (sch + scl)  (vv = v / (R N) when not compensated)
@@ -413,7 +418,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
     const float2* in = a.src + (size_t)z * N * N + SL * r;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -425,7 +430,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     // columns into this CTA's slice A[y][c]
     float2* A = smem;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
@@ -434,7 +439,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     cluster.sync();
     // rows 32r..: thread (row, j) takes kx = j + 16 k2 from slice k2/2
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NS; ++s) {
         const RowSlot q = row_slot(s);
         float2(&v)[16] = s ? v1 : v0;
         const int y = SL * r + q.row;
@@ -448,7 +453,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     fft256<true, true>(T, tw, v0, v1);
     // pointwise update on (x = 16 n1 + j, y, z)
     epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
-    epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
+    if (NS > 1) epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
     if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
