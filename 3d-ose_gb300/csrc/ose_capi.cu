@@ -60,6 +60,7 @@ struct ose_handle {
 
     // host copies
     std::vector<float> vb, h_ax, h_ay, h_az, h_ricker, h_hil;
+    std::vector<float> vel_in;   // the model as given ([x][y][z] interior); vb is padded from it on demand
     std::vector<double> J;
 
     long long src = 0;
@@ -69,6 +70,12 @@ struct ose_handle {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     ose::KernelTiming timing{};
+
+    // receiver rows on their way to the host (ose_run_record): two pinned
+    // chunks of kRecChunk rows and the events that mark them filled
+    float* rec_stage = nullptr;
+    int rec_stage_ng = 0;        // ng at allocation
+    cudaEvent_t rec_ev[2] = {nullptr, nullptr};
 
     // snapshots (allocated on first use): device copy of the state, two
     // pinned host buffers, a copy stream and its events
@@ -134,6 +141,9 @@ void free_all(ose_handle* h)
         if (h->snap_done[b]) cudaEventDestroy(h->snap_done[b]);
     }
     if (h->snap_ready) cudaEventDestroy(h->snap_ready);
+    if (h->rec_stage) cudaFreeHost(h->rec_stage);
+    for (int b = 0; b < 2; ++b)
+        if (h->rec_ev[b]) cudaEventDestroy(h->rec_ev[b]);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->corr) ose::learn::delete_corrector(h->corr);
     if (h->corr_vel) cudaFree(h->corr_vel);
@@ -343,6 +353,40 @@ ose_status tensor_status(ose_handle* h)
     return OSE_OK;
 }
 
+// The padded model [z][y][x] from the interior [x][y][z] (edge values
+// replicated into the sponge, as pad_model on the host), scaled by sc in
+// double and rounded to float (scale = false: v itself).
+__global__ void k_pad_model(const float* __restrict__ vin, float* __restrict__ vs, ose_params p, int nxb, int nyb,
+                            int nzb, double sc, bool scale)
+{
+    const long long n = (long long)nxb * nyb * nzb;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nxb), y = (int)((i / nxb) % nyb), z = (int)(i / ((long long)nxb * nyb));
+        const int ix = x < p.bl ? 0 : (x >= p.bl + p.nx ? p.nx - 1 : x - p.bl);
+        const int iy = y < p.bf ? 0 : (y >= p.bf + p.ny ? p.ny - 1 : y - p.bf);
+        const int iz = z < p.bu ? 0 : (z >= p.bu + p.nz ? p.nz - 1 : z - p.bu);
+        const float v = vin[((size_t)ix * p.ny + iy) * p.nz + iz];
+        vs[i] = scale ? (float)((double)v * sc) : v;
+    }
+}
+
+// P (which = 0) or Q (1) of the state, deinterleaved
+__global__ void k_take_component(const float2* __restrict__ W, float* __restrict__ out, long long n, int which)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 w = W[i];
+        out[i] = which ? w.y : w.x;
+    }
+}
+
+// The padded model on the host (pad_model of the model as given), made on
+// first use.
+const std::vector<float>& padded_model(ose_handle* h)
+{
+    if (h->vb.empty()) ose::pad_model(h->p, h->d, h->vel_in.data(), h->vb);
+    return h->vb;
+}
+
 void to_layout(const ose_handle* h, const float* zyx, float* out, int layout)
 {
     const int nxb = h->d.nxb, nyb = h->d.nyb, nzb = h->d.nzb;
@@ -446,12 +490,20 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     h->g.ncell = (long long)d.nxb * d.nyb * d.nzb;
     const size_t N = (size_t)h->g.ncell;
 
-    ose::pad_model(p, d, vel, h->vb);
+    // the padded model repeats the interior's values, so its maximum and its
+    // validity are the interior's
+    const size_t nin = (size_t)p.nx * p.ny * p.nz;
+    h->vel_in.assign(vel, vel + nin);
     float vmax = -9999999.999f;    // find_max (ose_3d_lib.cu:544-555)
-    for (float v : h->vb) vmax = v > vmax ? v : vmax;
-    if (!(vmax > 0.f) || !std::isfinite(vmax)) { delete h; return fail(nullptr, OSE_ERR_INVALID, "velocity model must be positive and finite"); }
-    for (float v : h->vb)
-        if (!(v > 0.f) || !std::isfinite(v)) { delete h; return fail(nullptr, OSE_ERR_INVALID, "velocity model must be positive and finite"); }
+    bool valid = true;
+    for (float v : h->vel_in) {
+        vmax = v > vmax ? v : vmax;
+        valid = valid && v > 0.f && std::isfinite(v);
+    }
+    if (!valid || !(vmax > 0.f) || !std::isfinite(vmax)) {
+        delete h;
+        return fail(nullptr, OSE_ERR_INVALID, "velocity model must be positive and finite");
+    }
     ose::series_params(p, vmax, &d);
     h->J.resize(d.M + 2);
     for (int n = 0; n <= d.M + 1; ++n) h->J[n] = jn(n, d.dtR);
@@ -515,14 +567,12 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(dalloc(h, &h->ctr, 4));
     CKC(dalloc(h, &h->tcerr, 1));
     CKC(cudaMemset(h->tcerr, 0, sizeof(int)));
-    if (ose::kCompensatedConstants) {
-        CKC(upload(h, h->vs, h->vb));
-    } else {
-        std::vector<float> vsc(N);
-        const double sc = 1.0 / (d.R * (double)N);
-        for (size_t i = 0; i < N; ++i) vsc[i] = (float)((double)h->vb[i] * sc);
-        CKC(upload(h, h->vs, vsc));
-    }
+    // the model as given goes up once (X is free scratch here) and is padded
+    // on the device; vs = v (compensated constants) or v / (R N)
+    CKC(cudaMemcpyAsync(h->X, h->vel_in.data(), sizeof(float) * nin, cudaMemcpyHostToDevice, h->stream));
+    k_pad_model<<<4096, 256, 0, h->stream>>>(reinterpret_cast<const float*>(h->X), h->vs, p, d.nxb, d.nyb, d.nzb,
+                                             1.0 / (d.R * (double)N), !ose::kCompensatedConstants);
+    CKC(cudaGetLastError());
     CKC(upload(h, h->twxl, twxl));
     CKC(upload(h, h->kx2l, kx2l));
     CKC(upload(h, h->ky2l, ky2l));
@@ -657,19 +707,53 @@ ose_status ose_run(ose_handle* h, int nsteps, float* gather_out)
     return OSE_OK;
 }
 
+// Steps are enqueued in chunks of kRecChunk without waiting on the host; each
+// chunk's receiver rows go to one of two pinned buffers by an asynchronous
+// copy, and the host moves chunk c into rows_out while chunk c + 1 runs.
+constexpr int kRecChunk = 32;
+
 ose_status ose_run_record(ose_handle* h, int nsteps, float* rows_out)
 {
-    if (!h || !rows_out) return OSE_ERR_INVALID;
+    if (!h || !rows_out || nsteps < 0) return OSE_ERR_INVALID;
+    if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
+    if (h->it + nsteps > h->p.nt) return fail(h, OSE_ERR_INVALID, "nsteps beyond nt");
     const int ng = h->d.ng;
-    for (int i = 0; i < nsteps; ++i) {
-        const int it = h->it;
-        ose_status s = run_graph(h, 1);
-        if (s != OSE_OK) return s;
-        CK(h, cudaMemcpyAsync(rows_out + (size_t)i * ng, h->gather + (size_t)it * ng, sizeof(float) * ng,
-                              cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaStreamSynchronize(h->stream));
-        h->it += 1;
+    if (!h->rec_stage || h->rec_stage_ng != ng) {
+        if (h->rec_stage) cudaFreeHost(h->rec_stage);
+        h->rec_stage = nullptr;
+        CK(h, cudaMallocHost((void**)&h->rec_stage, sizeof(float) * 2 * kRecChunk * (size_t)ng));
+        h->rec_stage_ng = ng;
     }
+    for (int b = 0; b < 2; ++b)
+        if (!h->rec_ev[b]) CK(h, cudaEventCreateWithFlags(&h->rec_ev[b], cudaEventDisableTiming));
+    const size_t chunk = (size_t)kRecChunk * ng;
+    int pending_k = 0, pending_b = 0;
+    float* pending_out = nullptr;
+    auto drain = [&]() -> ose_status {
+        if (!pending_k) return OSE_OK;
+        CK(h, cudaEventSynchronize(h->rec_ev[pending_b]));
+        memcpy(pending_out, h->rec_stage + pending_b * chunk, sizeof(float) * (size_t)pending_k * ng);
+        pending_k = 0;
+        return OSE_OK;
+    };
+    for (int done = 0, c = 0; done < nsteps; ++c) {
+        const int k = std::min(kRecChunk, nsteps - done), b = c & 1;
+        const int it0 = h->it;
+        ose_status s = run_graph(h, k);
+        if (s != OSE_OK) return s;
+        CK(h, cudaMemcpyAsync(h->rec_stage + b * chunk, h->gather + (size_t)it0 * ng, sizeof(float) * (size_t)k * ng,
+                              cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaEventRecord(h->rec_ev[b], h->stream));
+        h->it += k;
+        // chunk c - 1 (the other buffer) is complete or about to be
+        if ((s = drain()) != OSE_OK) return s;
+        pending_k = k;
+        pending_b = b;
+        pending_out = rows_out + (size_t)done * ng;
+        done += k;
+    }
+    ose_status s = drain();
+    if (s != OSE_OK) return s;
     return tensor_status(h);
 }
 
@@ -787,9 +871,9 @@ ose_status ose_set_corrector(ose_handle* h, const float* params, int shell)
         e = cudaMemcpy(ose::learn::net_of(h->corr).params, params, sizeof(float) * ose::learn::param_count(),
                        cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !h->corr_vel) {
-        e = cudaMalloc((void**)&h->corr_vel, sizeof(float) * h->vb.size());
-        if (e == cudaSuccess)
-            e = cudaMemcpy(h->corr_vel, h->vb.data(), sizeof(float) * h->vb.size(), cudaMemcpyHostToDevice);
+        const std::vector<float>& vb = padded_model(h);
+        e = cudaMalloc((void**)&h->corr_vel, sizeof(float) * vb.size());
+        if (e == cudaSuccess) e = cudaMemcpy(h->corr_vel, vb.data(), sizeof(float) * vb.size(), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess && !h->tcerr) {
         e = cudaMalloc((void**)&h->tcerr, sizeof(int));
@@ -1031,17 +1115,24 @@ ose_status ose_get_wavefield(ose_handle* h, int which, float* out, int layout)
     if (!h || !out) return OSE_ERR_INVALID;
     if (layout != OSE_LAYOUT_ZYX && layout != OSE_LAYOUT_YXZ) return fail(h, OSE_ERR_INVALID, "bad layout");
     const size_t N = (size_t)h->g.ncell;
-    std::vector<float> zyx(N);
     if (which == OSE_FIELD_V) {
-        zyx = h->vb;
-    } else if (which == OSE_FIELD_P || which == OSE_FIELD_Q) {
-        std::vector<float2> w(N);
-        CK(h, cudaMemcpyAsync(w.data(), h->W, sizeof(float2) * N, cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaStreamSynchronize(h->stream));
-        for (size_t i = 0; i < N; ++i) zyx[i] = which == OSE_FIELD_P ? w[i].x : w[i].y;
-    } else {
-        return fail(h, OSE_ERR_INVALID, "bad field");
+        to_layout(h, padded_model(h).data(), out, layout);
+        return OSE_OK;
     }
+    if (which != OSE_FIELD_P && which != OSE_FIELD_Q) return fail(h, OSE_ERR_INVALID, "bad field");
+    // one component, deinterleaved on the device into the scratch spectrum
+    // buffer (free between steps), then one copy of N floats
+    float* comp = reinterpret_cast<float*>(h->X);
+    k_take_component<<<4096, 256, 0, h->stream>>>(h->W, comp, (long long)N, which == OSE_FIELD_Q);
+    CK(h, cudaGetLastError());
+    if (layout == OSE_LAYOUT_ZYX) {
+        CK(h, cudaMemcpyAsync(out, comp, sizeof(float) * N, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        return OSE_OK;
+    }
+    std::vector<float> zyx(N);
+    CK(h, cudaMemcpyAsync(zyx.data(), comp, sizeof(float) * N, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
     to_layout(h, zyx.data(), out, layout);
     return OSE_OK;
 }

@@ -4,7 +4,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <complex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -108,6 +110,27 @@ void ricker_trace(int nt, float fm, float dt, float amp, std::vector<float>& out
 // k < nt/2 multiplied by -i and the rest by +i (hilbert_1d's test,
 // ose_3d_kernel.cu:158), unnormalised inverse real DFT.  The DC and, for even
 // nt, Nyquist bins turn purely imaginary and vanish from a real inverse.
+// Runs f(i) for i in [0, n) over up to 16 host threads (one when n is small).
+template <typename F>
+static void parallel_for(int n, F f)
+{
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int nth = n < 256 ? 1 : std::max(1, std::min(16, hw));
+    if (nth == 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t)
+        th.emplace_back([&, t] {
+            for (int i = t; i < n; i += nth) f(i);
+        });
+    for (auto& x : th) x.join();
+}
+
+// Direct DFTs in double with the exponent index advanced by addition
+// (j k mod nt), split over host threads by output index; the same
+// arithmetic for every thread count.
 void hilbert_trace(const std::vector<float>& w, int div_nt, std::vector<float>& out)
 {
     const int nt = (int)w.size();
@@ -118,27 +141,29 @@ void hilbert_trace(const std::vector<float>& w, int div_nt, std::vector<float>& 
         c[j] = cos(2.0 * M_PI * j / nt);
         s[j] = sin(2.0 * M_PI * j / nt);
     }
-    for (int k = 0; k < nb; ++k) {
+    parallel_for(nb, [&](int k) {
         double re = 0, im = 0;
-        for (int j = 0; j < nt; ++j) {
-            int e = (int)(((long long)j * k) % nt);
+        for (int j = 0, e = 0; j < nt; ++j) {
             re += w[j] * c[e];
             im -= w[j] * s[e];
+            e += k;
+            if (e >= nt) e -= nt;
         }
         std::complex<double> v(re, im);
         X[k] = k < nt / 2 ? v * std::complex<double>(0, -1) : v * std::complex<double>(0, 1);
-    }
+    });
     const int kmax = nt % 2 == 0 ? nt / 2 - 1 : (nt - 1) / 2;
     out.resize(nt);
-    for (int n = 0; n < nt; ++n) {
+    parallel_for(nt, [&](int n) {
         double acc = X[0].real();
         if (nt % 2 == 0) acc += X[nt / 2].real() * ((n & 1) ? -1.0 : 1.0);
-        for (int k = 1; k <= kmax; ++k) {
-            int e = (int)(((long long)k * n) % nt);
+        for (int k = 1, e = n % nt; k <= kmax; ++k) {
             acc += 2.0 * (X[k].real() * c[e] - X[k].imag() * s[e]);
+            e += n;
+            if (e >= nt) e -= nt;
         }
         out[n] = (float)(div_nt ? acc / nt : acc);
-    }
+    });
 }
 
 // Radix plan: 4s first, then 2, 3, 5, 7 and any remaining prime.
