@@ -81,6 +81,21 @@ __device__ __forceinline__ void tile_origin(int tp, int& x0, int& y0, int& z0)
 constexpr int kBoxR = 8;
 constexpr int kBoxTX = 32;   // x columns per block of the y and z passes
 
+// Which box sums are needed: s(x) only at shell cells, so the z pass writes
+// shell cells and reads the y pass where `need_y` holds, which reads the x
+// pass where `need_x` holds (each set holds the +-kBoxR neighbours the next
+// pass reads along its axis, periodic).
+__device__ __forceinline__ int edge_dist(int v, int n) { return min(v, n - 1 - v); }
+__device__ __forceinline__ bool need_y(const NetGeom& g, int x, int y, int z)
+{
+    return edge_dist(x, g.nx) < g.shell || edge_dist(y, g.ny) < g.shell || edge_dist(z, g.nz) < g.shell + kBoxR;
+}
+__device__ __forceinline__ bool need_x(const NetGeom& g, int x, int y, int z)
+{
+    return edge_dist(x, g.nx) < g.shell || edge_dist(y, g.ny) < g.shell + kBoxR ||
+           edge_dist(z, g.nz) < g.shell + kBoxR;
+}
+
 // rows of the x pass per block (shared memory <= 48 KiB)
 static int box_rows(const NetGeom& g) { return std::max(1, std::min(8, 12288 / (g.nx + 2 * kBoxR))); }
 static int box_blocks(const NetGeom& g)
@@ -104,14 +119,17 @@ __global__ void __launch_bounds__(256) k_box_x(const float2* __restrict__ W, flo
         const int r = i / L, j = i - r * L;
         const int row = row0 + r, y = row % g.ny, z = row / g.ny;
         const int x = wrapi(j - kBoxR, g.nx);
-        const float2 v = W[(size_t)row * g.nx + x];
-        const float e = in_shell(g, x, y, z) ? fmaf(v.x, v.x, v.y * v.y) : 0.f;
+        const bool sh = in_shell(g, x, y, z);
+        const float2 v = sh ? W[(size_t)row * g.nx + x] : make_float2(0.f, 0.f);
+        const float e = sh ? fmaf(v.x, v.x, v.y * v.y) : 0.f;
         box_e[i] = e;
         if (j >= kBoxR && j < g.nx + kBoxR) sum += e;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * g.nx; i += blockDim.x) {
         const int r = i / g.nx, x = i - r * g.nx;
+        const int row = row0 + r;
+        if (!need_x(g, x, row % g.ny, row / g.ny)) continue;
         const float* e = box_e + r * L + x;
         float acc = 0.f;
 #pragma unroll
@@ -156,30 +174,37 @@ __device__ __forceinline__ int modi(int v, int n) { return ((v % n) + n) % n; }
 // block per (x tile, plane index, chunk of kBoxL outputs): lines of length n
 // at stride `stride` (y pass: n = ny, stride nx, plane = z; z pass: n = nz,
 // stride nx ny, plane = y); the chunk and its periodic halo sit in shared
-// memory.  FINAL: s = sqrt(m / 2 + f^2), m the box mean, f = 1e-3 x the shell
-// RMS.
+// memory.  Only the sums the next step needs are read and written (need_x ->
+// need_y -> shell cells).  FINAL (the z pass): s = sqrt(m / 2 + f^2), m the
+// box mean, f = 1e-3 x the shell RMS.
 constexpr int kBoxL = 256;
 
 template <bool FINAL>
 __global__ void __launch_bounds__(256) k_box_lines(const float* __restrict__ in, float* __restrict__ out,
                                                    const float* __restrict__ scal, int n, long long stride,
-                                                   long long pstride, int nx)
+                                                   long long pstride, NetGeom g)
 {
     __shared__ float box_e[(kBoxL + 2 * kBoxR) * kBoxTX];
     const int c = threadIdx.x, x = blockIdx.x * kBoxTX + c;
     const int i0 = blockIdx.z * kBoxL, len = min(kBoxL, n - i0);
-    const size_t base = (size_t)blockIdx.y * pstride + x;
-    const bool ok = x < nx;
-    for (int j = threadIdx.y; j < len + 2 * kBoxR; j += blockDim.y)
-        box_e[j * kBoxTX + c] = ok ? in[base + (size_t)modi(i0 + j - kBoxR, n) * stride] : 0.f;
+    const int pl = blockIdx.y;
+    const size_t base = (size_t)pl * pstride + x;
+    const bool ok = x < g.nx;
+    for (int j = threadIdx.y; j < len + 2 * kBoxR; j += blockDim.y) {
+        const int i = modi(i0 + j - kBoxR, n);
+        const bool need = ok && (FINAL ? need_y(g, x, pl, i) : need_x(g, x, i, pl));
+        box_e[j * kBoxTX + c] = need ? in[base + (size_t)i * stride] : 0.f;
+    }
     __syncthreads();
     if (!ok) return;
     const float f = FINAL ? 1e-3f * scal[1] : 0.f;
     const float inv_vol = 1.f / (float)((2 * kBoxR + 1) * (2 * kBoxR + 1) * (2 * kBoxR + 1));
     for (int j = threadIdx.y; j < len; j += blockDim.y) {
+        const int i = i0 + j;
+        if (!(FINAL ? in_shell(g, x, pl, i) : need_y(g, x, i, pl))) continue;
         float acc = 0.f;
         for (int d = 0; d <= 2 * kBoxR; ++d) acc += box_e[(j + d) * kBoxTX + c];
-        out[base + (size_t)(i0 + j) * stride] = FINAL ? sqrtf(0.5f * fmaxf(acc, 0.f) * inv_vol + f * f) : acc;
+        out[base + (size_t)i * stride] = FINAL ? sqrtf(0.5f * fmaxf(acc, 0.f) * inv_vol + f * f) : acc;
     }
 }
 
@@ -531,9 +556,9 @@ cudaError_t shell_scale(cudaStream_t s, const Net& n, const float2* W)
     k_box_x<<<nb, 256, sizeof(float) * rows * (g.nx + 2 * kBoxR), s>>>(W, n.sloc, part, g, rows);
     k_shell_scale<<<1, 1024, 0, s>>>(n.scal, part, nb, (float)(0.5 / (double)std::max(1LL, n.ncells)));
     k_box_lines<false><<<dim3(xt, g.nz, (g.ny + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
-        n.sloc, n.stmp, n.scal, g.ny, g.nx, plane, g.nx);
+        n.sloc, n.stmp, n.scal, g.ny, g.nx, plane, g);
     k_box_lines<true><<<dim3(xt, g.ny, (g.nz + kBoxL - 1) / kBoxL), dim3(kBoxTX, 8), 0, s>>>(
-        n.stmp, n.sloc, n.scal, g.nz, plane, g.nx, g.nx);
+        n.stmp, n.sloc, n.scal, g.nz, plane, g.nx, g);
     return cudaGetLastError();
 }
 

@@ -13,12 +13,13 @@
 // (taps dz = -1, 0, +1), so the B operand of a tap (dx, dy) holds the three
 // dz weight blocks side by side and one MMA of N = 3 Cout updates the three
 // output planes' accumulators, which sit next to one another in a ring of
-// eight accumulators in TMEM: each halo plane is read by the tensor core 9
-// times instead of 27.  The global loads of the next halo plane are in flight
-// while the CTA writes out the plane that the last MMAs completed.
+// accumulators in TMEM (an MMA is split in two where the run wraps): each
+// halo plane is read by the tensor core 9 times instead of 27.  The global
+// loads of the next halo plane are in flight while the CTA writes out the
+// plane that the last MMAs completed.
 //
-// Layer 0's halo is built from the state and the velocity (the 8 features,
-// padded to 16 channels with zeros); hidden activations are BF16 [cell][32];
+// Layer 0's halo is built from the state and the velocity (the 8 features;
+// K = 16 pairs two x taps, see LayerCfg); hidden activations are BF16 [cell][32];
 // the output layer adds s(x) (dP, dQ) to the state at the write cells.  Inputs
 // outside the shell are zero, as in the FP32 kernels (ose_learn.cu).
 #include <cuda_bf16.h>
@@ -42,7 +43,7 @@ constexpr int TXW = 8, TYW = 16;              // output tile (x, y) of one z pla
 constexpr int HX = TXW + 2, HY = TYW + 2;
 constexpr int ZL = 16;                        // output planes per column at most
 constexpr int SLOTS = 2;                      // halo plane slots per pipeline
-constexpr int RING = 4;                       // accumulators (output planes) per pipeline in TMEM
+constexpr int TMEM_PER_PIPE = 128;            // TMEM columns per pipeline (4 pipelines per SM)
 constexpr int kMinSmem = 80 * 1024;           // at most two CTAs per SM (their TMEM)
 constexpr int PIPE_THREADS = 128;             // one output row (cell) per thread
 constexpr int PIPES = 2;                      // independent columns per CTA (shared weights)
@@ -79,28 +80,40 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     return u;
 }
 
+// Layer 0 (CIN = 16: 8 features + 8 zero channels) uses PAIR taps: its halo
+// has one 16-byte chunk per cell in rows of 11 cells (the 11th zero), and an
+// A descriptor with LBO = 16 bytes reads K channels 8..15 from the next cell
+// in x, so one K = 16 MMA applies two x taps (dx, dx + 1): 3 dy x 2 pairs
+// ((-1, 0) and (+1, +2 with zero weights)) instead of 9 taps.
 template <int CIN, int NPAD>
 struct LayerCfg {
-    static constexpr int chunks = CIN / 8;                       // 16-byte channel chunks
-    static constexpr int plane_bytes = HY * chunks * HX * 16;    // one halo plane
+    static constexpr bool pair = CIN == 16;
+    static constexpr int chunks = pair ? 1 : CIN / 8;            // 16-byte chunks per halo cell
+    static constexpr int hxp = pair ? HX + 1 : HX;               // halo row length in cells
+    static constexpr int plane_bytes = HY * chunks * hxp * 16;   // one halo plane
     static constexpr int halo_bytes = PIPES * SLOTS * plane_bytes;
-    static constexpr uint32_t lbo = HX * 16;                     // chunk stride in a plane
-    static constexpr uint32_t sbo = chunks * HX * 16;            // y stride in a plane
+    static constexpr uint32_t lbo = pair ? 16 : hxp * 16;        // A: K chunk stride
+    static constexpr uint32_t sbo = chunks * hxp * 16;           // A: y stride
+    static constexpr int kchunks = CIN / 8;                      // B: K chunks
+    static constexpr int ntaps = pair ? 6 : 9;                   // B blocks: (dy, pair) or (dx, dy)
     static constexpr int ngroups = 3 * NPAD / 8;                 // B rows: dz = +1, 0, -1 blocks
-    static constexpr int tap_bytes = ngroups * chunks * 128;     // B operand of one (dx, dy)
-    static constexpr int w_bytes = 9 * tap_bytes;
-    static constexpr uint32_t wsbo = chunks * 128;               // B: n-group stride
+    static constexpr int tap_bytes = ngroups * kchunks * 128;    // B operand of one tap
+    static constexpr int w_bytes = ntaps * tap_bytes;
+    static constexpr uint32_t wsbo = kchunks * 128;              // B: n-group stride
     static constexpr int ksteps = CIN / 16;
     static constexpr int off_w = halo_bytes;
     static constexpr int off_bias = off_w + w_bytes;
     static constexpr int off_bar = off_bias + NPAD * 4;          // 2 mbarriers per pipeline, TMEM address
     static constexpr int used = off_bar + 8 * 2 * PIPES + 8;
     static constexpr int smem = used > kMinSmem ? used : kMinSmem;
-    static constexpr int tmem_cols = PIPES * RING * NPAD;
+    // ring of accumulators (output planes) per pipeline: 4 of 32 columns, or
+    // 8 of 16 for the output layer (a run of three wraps less often)
+    static constexpr int ring = TMEM_PER_PIPE / NPAD;
+    static constexpr int tmem_cols = PIPES * TMEM_PER_PIPE;
     // staged loads of one halo plane per thread: cells (layer 0) or 16-byte units
     static constexpr int cells = HY * HX;
     static constexpr int units = cells * chunks;
-    static constexpr int per = ((CIN == 16 ? cells : units) + PIPE_THREADS - 1) / PIPE_THREADS;
+    static constexpr int per = ((pair ? cells : units) + PIPE_THREADS - 1) / PIPE_THREADS;
 };
 
 // One halo plane in registers: layer 0 keeps the state, velocity and scale of
@@ -157,9 +170,7 @@ __device__ __forceinline__ void store_plane(const Staged<MODE, LayerCfg<CIN, NPA
             v.y = pack2(st.v[k] * (1.f / 4500.f), face_coord(x, g.nx, g.shell));
             v.z = pack2(face_coord(y, g.ny, g.shell), face_coord(z, g.nz, g.shell));
         }
-        *reinterpret_cast<uint4*>(slot + ((hy * C::chunks + ch) * HX + hx) * 16) = v;
-        if (MODE == 0)   // channels 8..15 of layer 0 are zero padding
-            *reinterpret_cast<uint4*>(slot + ((hy * C::chunks + 1) * HX + hx) * 16) = make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4*>(slot + ((hy * C::chunks + ch) * C::hxp + hx) * 16) = v;
     }
 }
 
@@ -221,11 +232,14 @@ __global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restri
         int4* d4 = reinterpret_cast<int4*>(sm + C::off_w);
         for (int i = t; i < C::w_bytes / 16; i += THREADS) d4[i] = s4[i];
         for (int i = t; i < NPAD; i += THREADS) sb[i] = bias[i];
+        if (C::pair)   // the 11th cell of every halo row: read by the (+1, +2) pair, never loaded
+            for (int i = t; i < PIPES * SLOTS * HY; i += THREADS)
+                *reinterpret_cast<uint4*>(sm + (size_t)i * C::hxp * 16 + HX * 16) = make_uint4(0, 0, 0, 0);
     }
     tc5::fence_before_sync();
     __syncthreads();
     tc5::fence_after_sync();
-    const uint32_t tmem = *tslot + (uint32_t)(pipe * RING * NPAD);
+    const uint32_t tmem = *tslot + (uint32_t)(pipe * TMEM_PER_PIPE);
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     int failed = 0;
     uint32_t ph = 0u;   // bit b: the parity to wait for on bar[b]
@@ -270,8 +284,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restri
     // q - (p - 2))
     auto issue = [&](int p, int qa, int qb, uint64_t da, uint32_t b0, uint32_t acc) {
         while (qa <= qb) {
-            const int s = qa & (RING - 1);
-            const int cnt = min(qb - qa + 1, RING - s);
+            const int s = qa & (C::ring - 1);
+            const int cnt = min(qb - qa + 1, C::ring - s);
             const int blk = qa - (p - 2);
             const uint64_t db = tc5::smem_desc(b0 + blk * (NPAD / 8) * C::wsbo, 128, C::wsbo);
             tc5::mma_f16(tmem + (uint32_t)(s * NPAD), da, db, tc5::idesc(tc5::kTypeBF16, 128, cnt * NPAD), acc);
@@ -300,9 +314,11 @@ __global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restri
                 const int qa = max(p - 2, 0), qb = min(p, len - 1);
                 const bool fresh = p <= len - 1;   // output p starts here
                 const uint32_t slot = hbase + (p & 1) * C::plane_bytes;
-                for (int tap = 0; tap < 9; ++tap) {
-                    const int dx = tap % 3 - 1, dy = tap / 3 - 1;
-                    const uint32_t a0 = slot + (1 + dy) * C::sbo + (1 + dx) * 16;
+                for (int tap = 0; tap < C::ntaps; ++tap) {
+                    // halo x of the A rows' first tap: dx + 1, or 0 / 2 for the pairs
+                    const int dy = C::pair ? tap / 2 - 1 : tap / 3 - 1;
+                    const int hx0 = C::pair ? 2 * (tap & 1) : tap % 3;
+                    const uint32_t a0 = slot + (1 + dy) * C::sbo + hx0 * 16;
                     const uint32_t b0 = wbase + tap * C::tap_bytes;
 #pragma unroll
                     for (int k = 0; k < C::ksteps; ++k) {
@@ -324,7 +340,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restri
                 bad = !tc5::mbar_wait(bar + b, (ph >> b) & 1u, kWaitLimitNs);
                 if (!bad) ph ^= 1u << b;
                 tc5::fence_after_sync();
-                if (!bad && p >= 3) epilogue(x0, y0, z0 + p - 3, (p - 3) & (RING - 1));
+                if (!bad && p >= 3) epilogue(x0, y0, z0 + p - 3, (p - 3) & (C::ring - 1));
             }
             if (p <= len) store_plane<CIN, NPAD, MODE>(st, halo + ((p + 1) & 1) * C::plane_bytes, g, x0, y0, zn, tl);
         }
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_conv_tc(const uint16_t* __restri
             bad = !tc5::mbar_wait(bar + b, (ph >> b) & 1u, kWaitLimitNs);
             if (!bad) ph ^= 1u << b;
             tc5::fence_after_sync();
-            if (!bad) epilogue(x0, y0, z0 + len - 1, (len - 1) & (RING - 1));
+            if (!bad) epilogue(x0, y0, z0 + len - 1, (len - 1) & (C::ring - 1));
         }
         tc5::fence_before_sync();
         failed = pipe_sync_or(pipe, bad);
@@ -364,21 +380,36 @@ uint16_t bf16_bits(float f)
 }  // namespace
 
 // Host: BF16 B operands of one layer in the kernel's shared-memory layout
-// [dx, dy][n group][channel chunk][8 rows][8 channels], row n = blk * npad +
+// [tap][n group][channel chunk][8 rows][8 channels], row n = blk * npad +
 // output channel with blk 0, 1, 2 the taps dz = +1, 0, -1; zero beyond
-// (cin, cout).  w: [tap = (dz + 1) 9 + (dy + 1) 3 + dx + 1][cin][cout].
+// (cin, cout).  Taps: (dx, dy) = tap % 3 - 1, tap / 3 - 1, or for layer 0
+// (cin_pad 16, pairs) dy = tap / 2 - 1 with K 0..7 the x tap dx_a = -1 or
+// +1 (tap & 1) and K 8..15 the tap dx_a + 1 (zero for +2).
+// w: [tap = (dz + 1) 9 + (dy + 1) 3 + dx + 1][cin][cout].
 void tc_layer_weights(const float* w, int cin, int cout, int cin_pad, int npad, std::vector<uint8_t>& out)
 {
-    const int chunks = cin_pad / 8, ngroups = 3 * npad / 8;
-    out.assign((size_t)9 * ngroups * chunks * 128, 0);
-    for (int dxy = 0; dxy < 9; ++dxy)
+    const bool pair = cin_pad == 16;
+    const int kchunks = cin_pad / 8, ngroups = 3 * npad / 8, ntaps = pair ? 6 : 9;
+    out.assign((size_t)ntaps * ngroups * kchunks * 128, 0);
+    for (int tap = 0; tap < ntaps; ++tap)
         for (int n = 0; n < 3 * npad; ++n)
             for (int k = 0; k < cin_pad; ++k) {
                 const int blk = n / npad, co = n % npad, dz = 1 - blk;
-                const int tap = (dz + 1) * 9 + dxy;
-                const float v = (co < cout && k < cin) ? w[((size_t)tap * cin + k) * cout + co] : 0.f;
+                int dx, dy, ci;
+                if (pair) {
+                    dy = tap / 2 - 1;
+                    dx = 2 * (tap & 1) - 1 + k / 8;
+                    ci = k % 8;
+                } else {
+                    dx = tap % 3 - 1;
+                    dy = tap / 3 - 1;
+                    ci = k;
+                }
+                const bool live = co < cout && ci < cin && dx <= 1;
+                const int src = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+                const float v = live ? w[((size_t)src * cin + ci) * cout + co] : 0.f;
                 const uint16_t b = bf16_bits(v);
-                const size_t o = (((size_t)dxy * ngroups + n / 8) * chunks + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+                const size_t o = (((size_t)tap * ngroups + n / 8) * kchunks + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
                 memcpy(out.data() + o, &b, 2);
             }
 }
