@@ -229,13 +229,15 @@ cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
     ea.nx = D.nx;
     ea.ny = D.ny;
     ea.nt = D.nt;
+    const bool fuse = ose::generic_fuses_x(D.px);   // as the single-shot step
     for (int n = 0; n <= D.M; ++n) {
         const float2* an = n == 0 ? D.W : ((n & 1) ? D.A : D.W);
         ea.prev = n == 0 ? D.A : ((n & 1) ? D.W : D.A);
         ea.c1 = D.c[n];
         ea.c1l = D.cl[n];
         const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == D.M ? ose::EPI_LAST : ose::EPI_MID);
-        e = ose::launch_generic_application(st, D.g, D.px, D.py, D.pz, t, an, D.X, mode, ea, nullptr);
+        e = ose::launch_generic_application(st, D.g, D.px, D.py, D.pz, t, an, D.X, mode, ea, nullptr,
+                                            fuse && n > 0, fuse && n < D.M);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -304,17 +304,26 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = tru
     ea.w = h->W;
     ose::split_float(h->J[0], &ea.c0, &ea.c0l);
     ose::split_float(2.0 * h->J[1], &ea.c1, &ea.c1l);
+    // with the register row kernels, the row pass of application n also
+    // writes the x transform of a_{n+1}, so application n + 1 skips its x pass
+    const bool fuse = ose::generic_fuses_x(h->px);
     e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->W, h->X,
-                                        ose::EPI_FIRST, ea, tm);
-    if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += 36.0 * N; }
+                                        ose::EPI_FIRST, ea, tm, false, fuse && M > 0);
+    if (tm) {
+        for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N;
+        tm->bytes[4] += (fuse && M > 0 ? 44.0 : 36.0) * N;
+    }
     if (e != cudaSuccess) return e;
     for (int n = 1; n <= M; ++n) {
         const float2* an = (n & 1) ? h->A : h->W;
         ea.prev = (n & 1) ? h->W : h->A;
         ose::split_float(2.0 * h->J[n + 1], &ea.c1, &ea.c1l);
         e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, an, h->X,
-                                            n == M ? ose::EPI_LAST : ose::EPI_MID, ea, tm);
-        if (tm) { for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N; tm->bytes[4] += (n == M ? 36.0 : 44.0) * N; }
+                                            n == M ? ose::EPI_LAST : ose::EPI_MID, ea, tm, fuse, fuse && n < M);
+        if (tm) {
+            for (int c = fuse ? 1 : 0; c < 4; ++c) tm->bytes[c] += 16.0 * N;
+            tm->bytes[4] += (n == M ? 36.0 : (fuse ? 52.0 : 44.0)) * N;
+        }
         if (e != cudaSuccess) return e;
     }
     if (source && (e = enqueue_receivers(h, tm)) != cudaSuccess) return e;

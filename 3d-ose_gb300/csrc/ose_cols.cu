@@ -262,8 +262,10 @@ struct RowCfg {
 
 // x rows (contiguous, row = z * nyb + y) of row block rb.  EPI_NONE: forward
 // transform of src into dst.  Otherwise: inverse transform of src followed by
-// epilogue<EPI>.
-template <int C, int EPI>
+// epilogue<EPI>; FWD (FIRST, MID): then the forward transform of the new term
+// a_{n+1}, still in registers, into dst (the next application's x pass; each
+// row is read before it is written, by the same CTA).
+template <int C, int EPI, bool FWD = false>
 __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2* __restrict__ dst, int nyb,
                                          long long nrows, const float2* __restrict__ twg, const EpiArgs& e,
                                          long long rb, float2* W, float2* T)
@@ -316,19 +318,36 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
             for (int k1 = 0; k1 < 16; ++k1) v[k1] = Tr[q * 17 + k1];
             dftc<16, C, true>(v, W);
             const int y = (int)(row % nyb), z = (int)(row / nyb);
-            epilogue_row<EPI, 16>(v, row * N + q, q, C, y, z, e);
+            epilogue_row<EPI, 16, FWD>(v, row * N + q, q, C, y, z, e);
+            if (FWD) {   // forward phase 1 of a_{n+1} (v[n1] = a[C n1 + j]); thread q owns Tr row q
+                dftc<16, C, false>(v, W);
+#pragma unroll
+                for (int k1 = 0; k1 < 16; ++k1) Tr[q * 17 + k1] = k1 ? cmul(v[k1], W[q * k1]) : v[k1];
+            }
+        }
+        if (FWD) {
+            __syncthreads();
+            if (q < 16 && ok) {   // forward phase 2
+                float2 u[C];
+#pragma unroll
+                for (int j = 0; j < C; ++j) u[j] = Tr[j * 17 + q];
+                dftc<C, 16, false>(u, W);
+                float2* out = dst + row * N + q;
+#pragma unroll
+                for (int k2 = 0; k2 < C; ++k2) out[16 * k2] = u[k2];
+            }
         }
     }
 }
 
-template <int C, int EPI>
+template <int C, int EPI, bool FWD = false>
 __global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
                                                             int nyb, long long nrows, const float2* __restrict__ twg,
                                                             EpiArgs e)
 {
     extern __shared__ float4 smem4[];
     float2* W = reinterpret_cast<float2*>(smem4);
-    row_body<C, EPI>(src, dst, nyb, nrows, twg, e, blockIdx.x, W, W + RowCfg<C>::N);
+    row_body<C, EPI, FWD>(src, dst, nyb, nrows, twg, e, blockIdx.x, W, W + RowCfg<C>::N);
 }
 
 // Batched x rows of application n: forward (a_n -> X) or inverse + the series
@@ -354,13 +373,13 @@ __global__ void __launch_bounds__(RowCfg<C>::THREADS) kb_row(const BatchShot* __
     else row_body<C, EPI_MID>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
 }
 
-template <int C, int EPI>
+template <int C, int EPI, bool FWD = false>
 cudaError_t launch_row_one(cudaStream_t s, const float2* src, float2* dst, int nyb, long long nrows,
                            const float2* twg, const EpiArgs& e)
 {
     using K = RowCfg<C>;
     const unsigned grid = (unsigned)((nrows + K::RW - 1) / K::RW);
-    k_row<C, EPI><<<grid, K::THREADS, K::SMEM, s>>>(src, dst, nyb, nrows, twg, e);
+    k_row<C, EPI, FWD><<<grid, K::THREADS, K::SMEM, s>>>(src, dst, nyb, nrows, twg, e);
     return cudaGetLastError();
 }
 
@@ -375,6 +394,8 @@ cudaError_t launch_row_c(cudaStream_t s, int epi, const float2* src, float2* dst
     case EPI_LAST: return launch_row_one<C, EPI_LAST>(s, src, dst, nyb, nrows, twg, e);
     case EPI_SCALE: return launch_row_one<C, EPI_SCALE>(s, src, dst, nyb, nrows, twg, e);
     case EPI_SCALE_VEL: return launch_row_one<C, EPI_SCALE_VEL>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_FIRST_FWD: return launch_row_one<C, EPI_FIRST, true>(s, src, dst, nyb, nrows, twg, e);
+    case EPI_MID_FWD: return launch_row_one<C, EPI_MID, true>(s, src, dst, nyb, nrows, twg, e);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -11,7 +11,9 @@
 namespace ose {
 
 // EPI_SCALE_VEL: out = X * vel[i] * scale (the allocation-free entry point)
-enum { EPI_NONE = -1, EPI_SCALE_VEL = 4 };
+// EPI_FIRST_FWD, EPI_MID_FWD (row launches only): FIRST / MID followed by the
+// next application's forward x transform of the new term.
+enum { EPI_NONE = -1, EPI_SCALE_VEL = 4, EPI_FIRST_FWD = 5, EPI_MID_FWD = 6 };
 
 // The pointwise work of one application on cell i = (x, y, z); X is the
 // unnormalised inverse transform, e.vs the velocity, (e.sch + e.scl) = 1/(R N).
@@ -66,7 +68,9 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
 // The same work for cnt cells of one row held by one thread, x = x0 + k * xs,
 // i = i0 + k * xs: every load of a chunk of 8 cells is issued before the
 // first store, so the loads overlap (the per-cell arithmetic is epilogue's).
-template <int EPI, int CNT>
+// KEEP (FIRST, MID): v also receives the new term a_{n+1}, for the next
+// application's forward transform in the same kernel.
+template <int EPI, int CNT, bool KEEP = false>
 __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int x0, int xs, int y, int z,
                                              const EpiArgs& e)
 {
@@ -113,6 +117,7 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
                                          fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
                 else
                     e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+                if (KEEP) v[k] = a1;
             } else {
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
                 const float att = axv[q] * ayz0 * ayz1;
@@ -126,6 +131,7 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
                 if (EPI == EPI_MID) {
                     e.prev[i] = an;
                     e.S[i] = s;
+                    if (KEEP) v[k] = an;
                 } else {
                     e.wout[i] = s;
                     if (z == e.gz) {

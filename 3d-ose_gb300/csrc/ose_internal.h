@@ -86,10 +86,16 @@ inline void split_float(double v, float* hi, float* lo)
 
 // Host-side launch helpers (ose_kernels.cu).
 struct KernelTiming;
+// One operator application with the series update (5 passes).  With the
+// register row kernels (generic_fuses_x): x_ready = X already holds the x
+// transform of an (pass 1 skipped); fwd_next (FIRST, MID) = the row pass also
+// writes the x transform of the new term into X for the next application.
+bool generic_fuses_x(const AxisPlan& px);
 cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                        const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                        const float2* an, float2* X, EpiMode mode,
-                                       const EpiArgs& e, KernelTiming* timing);
+                                       const EpiArgs& e, KernelTiming* timing, bool x_ready = false,
+                                       bool fwd_next = false);
 cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float* ricker,
                           const float* hil, int* ctr, int nt);
 cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisPlan& px,

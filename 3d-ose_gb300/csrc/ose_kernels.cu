@@ -280,13 +280,15 @@ cudaError_t configure_kernels()
 // Timing classes of the generic path.
 enum { T_XF = 0, T_YF = 1, T_ZK = 2, T_YI = 3, T_XI = 4, T_INJ = 5 };
 
+// x_ready: X already holds the forward x transform of a_n (written by the
+// previous application's fused row pass), so pass 1 is skipped.
 static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                  const AxisPlan& py, const AxisPlan& pz, const Tables& t,
-                                 const float2* an, float2* X, KernelTiming* tm)
+                                 const float2* an, float2* X, KernelTiming* tm, bool x_ready = false)
 {
     EpiArgs none{};
     const long long nrows = (long long)g.nyb * g.nzb;
-    {
+    if (!x_ready) {
         Timer T(tm, s, T_XF);
         if (use_col_kernels() && col_supported(px.n)) {
             cudaError_t e = launch_row(s, EPI_NONE, px.n, an, X, g.nyb, nrows, t.twx, none);
@@ -343,19 +345,25 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     return cudaGetLastError();
 }
 
+bool generic_fuses_x(const AxisPlan& px) { return use_col_kernels() && col_supported(px.n); }
+
 cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                        const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                        const float2* an, float2* X, EpiMode mode, const EpiArgs& e,
-                                       KernelTiming* tm)
+                                       KernelTiming* tm, bool x_ready, bool fwd_next)
 {
-    cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, an, X, tm);
+    const bool fuse = generic_fuses_x(px);
+    cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, an, X, tm, fuse && x_ready);
     if (err != cudaSuccess) return err;
     const long long nrows = (long long)g.nyb * g.nzb;
     const int rpc = rows_per_cta(px.n);
     const unsigned nb = (unsigned)((nrows + rpc - 1) / rpc);
     Timer T(tm, s, T_XI);
-    if (use_col_kernels() && col_supported(px.n)) {
-        err = launch_row(s, (int)mode, px.n, X, nullptr, g.nyb, nrows, t.twx, e);
+    if (fuse) {
+        int epi = (int)mode;
+        if (fwd_next && mode == EPI_FIRST) epi = EPI_FIRST_FWD;
+        if (fwd_next && mode == EPI_MID) epi = EPI_MID_FWD;
+        err = launch_row(s, epi, px.n, X, X, g.nyb, nrows, t.twx, e);
         T.done();
         return err;
     }
