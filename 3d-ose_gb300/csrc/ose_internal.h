@@ -127,6 +127,10 @@ bool plane_path_supported(int nxb, int nyb, int nzb);
 cudaError_t configure_plane_kernels();
 cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, const Tables& t);
 cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t);
+// The same z pass (forward, |k|, inverse of 256-point z lines) on any grid
+// with 256 z planes and nxb a multiple of 16.
+bool zpass256_supported(const Geometry& g);
+cudaError_t launch_zpass256(cudaStream_t s, float2* X, const Geometry& g, const Tables& t);
 cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float2* Xin, float2* Xout,
                              const Tables& t, const EpiArgs& e);
 cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,

@@ -320,6 +320,9 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
         if (t.tcvar != OSE_PRECISION_FP32) {
             cudaError_t e = launch_tensor_zpass(s, X, g, t);
             if (e != cudaSuccess) return e;
+        } else if (use_col_kernels() && zpass256_supported(g)) {
+            cudaError_t e = launch_zpass256(s, X, g, t);
+            if (e != cudaSuccess) return e;
         } else if (zcols) {
             cudaError_t e = launch_col(s, 2, pz.n, X, g.nxb, g.nyb, plane, g.nxb, t.twz, t);
             if (e != cudaSuccess) return e;

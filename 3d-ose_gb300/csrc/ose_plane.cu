@@ -474,8 +474,10 @@ __device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, f
     l = e + al + bl;
 }
 
+// Any grid with 256 z planes and nxb a multiple of 16 (row stride nxb, plane
+// stride nxb * nyb): the plane path's z pass and the generic path's.
 __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
-                                                         Tables t)
+                                                         Tables t, int nxb, long long plane)
 {
     extern __shared__ float4 smem4[];
     float2* T = reinterpret_cast<float2*>(smem4);
@@ -483,8 +485,7 @@ __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X,
     load_twiddles(tw, gtw, t.twl);
     const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
     const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
-    float2* base = X + (size_t)ky * N + kx;
-    const size_t plane = (size_t)N * N;
+    float2* base = X + (size_t)ky * nxb + kx;
     float2 v[16];
 #pragma unroll
     for (int n1 = 0; n1 < 16; ++n1) v[n1] = base[(size_t)(16 * n1 + j) * plane];
@@ -581,7 +582,17 @@ cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
         Geometry g{plane::N, plane::N, plane::N, (long long)plane::N * plane::N * plane::N};
         return launch_tensor_zpass(s, X, g, t);
     }
-    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(X, t.twx, t);
+    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
+        X, t.twx, t, plane::N, (long long)plane::N * plane::N);
+    return cudaGetLastError();
+}
+
+bool zpass256_supported(const Geometry& g) { return g.nzb == plane::N && g.nxb % plane::ZW == 0; }
+
+cudaError_t launch_zpass256(cudaStream_t s, float2* X, const Geometry& g, const Tables& t)
+{
+    plane::k_zpass16<<<dim3(g.nxb / plane::ZW, g.nyb), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
+        X, t.twz, t, g.nxb, (long long)g.nxb * g.nyb);
     return cudaGetLastError();
 }
 
