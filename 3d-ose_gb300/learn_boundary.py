@@ -152,7 +152,9 @@ def generate(runs: int, seed: int, n: int = 48, steps: int = 150, t0: int = 20, 
     return dict(X=X[:i], Y=Y[:i], V=V, run=run_of[:i], n=n)
 
 
-def train(data, epochs: int = 4, batch: int = 16, lr: float = 1e-3, seed: int = 0, log=print):
+def train(data, epochs: int = 4, batch: int = 16, lr: float = 1e-3, seed: int = 0, log=print, init=None):
+    """Adam with cosine decay over `epochs` passes of the samples, from the
+    seeded initialisation or from `init` (parameters to continue from)."""
     import torch
     X, Y, V, run = data["X"], data["Y"], data["V"], data["run"]
     S = X.shape[0]
@@ -160,7 +162,7 @@ def train(data, epochs: int = 4, batch: int = 16, lr: float = 1e-3, seed: int = 
     rng = np.random.default_rng(seed)
     hist = []
     with ose3d.Corrector((nb, nb, nb), (THIN,) * 6, shell=SHELL) as c:
-        c.set_params(init_params(seed))
+        c.set_params(init_params(seed) if init is None else np.asarray(init, np.float32))
         steps = epochs * (S // batch)
         k = 0
         t_start = time.time()
@@ -236,6 +238,7 @@ def main():
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=1234)
     t.add_argument("--out", default=WEIGHTS)
+    t.add_argument("--init", default=None, help="continue from these parameters (.npy)")
     e = sub.add_parser("eval")
     e.add_argument("--weights", default=WEIGHTS)
     e.add_argument("--cases", type=int, default=4)
@@ -247,7 +250,8 @@ def main():
         t0 = time.time()
         data = generate(a.runs, a.seed, n=a.n, steps=a.steps, every=a.every)
         t_gen = time.time() - t0
-        params, hist = train(data, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed)
+        params, hist = train(data, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed,
+                             init=np.load(a.init) if a.init else None)
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
         np.save(a.out, params)
         print(json.dumps({"samples": int(data["X"].shape[0]), "runs": a.runs, "generate_s": round(t_gen, 1),
