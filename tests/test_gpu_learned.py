@@ -1,7 +1,7 @@
 """The trained boundary corrector (3d-ose_gb300/weights/corrector.npy, made by
 learn_boundary.py train: 200 solver pairs, interior 48^3, 8- vs 64-cell
 sponge) on held-out cases: the thin-sponge run with the corrector against the
-same run without it, both judged by the 64-cell-sponge run.
+same run without it, both measured against the 64-cell-sponge run.
 
 Measured when the weights were made (4 held-out cases, 300 steps): interior
 error energy 0.24-0.42 without, 0.022-0.050 with the corrector (gain 8-11x);
