@@ -474,10 +474,14 @@ __device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, f
     l = e + al + bl;
 }
 
-// Any grid with 256 z planes and nxb a multiple of 16 (row stride nxb, plane
-// stride nxb * nyb): the plane path's z pass and the generic path's.
+// GRID: any grid with 256 z planes and nxb a multiple of 16 (row stride
+// nxb, plane stride nxb * nyb as arguments: the generic path's z pass);
+// otherwise the 256^3 plane path's, with the strides as constants (runtime
+// strides cost registers: the GRID form spills a little at this bound, which
+// measured faster than three CTAs per SM without most of the spills).
+template <bool GRID>
 __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
-                                                         Tables t, int nxb, long long plane)
+                                                         Tables t, int nxb_arg, long long plane_arg)
 {
     extern __shared__ float4 smem4[];
     float2* T = reinterpret_cast<float2*>(smem4);
@@ -485,6 +489,8 @@ __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X,
     load_twiddles(tw, gtw, t.twl);
     const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
     const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
+    const int nxb = GRID ? nxb_arg : N;
+    const size_t plane = GRID ? (size_t)plane_arg : (size_t)N * N;
     float2* base = X + (size_t)ky * nxb + kx;
     float2 v[16];
 #pragma unroll
@@ -560,7 +566,8 @@ cudaError_t configure_plane_kernels()
     ALLOW((plane::k_plane_inv<EPI_LAST, false>));
     ALLOW((plane::k_plane_inv<EPI_MID, false>));
     ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
-    ALLOW(plane::k_zpass16);
+    ALLOW(plane::k_zpass16<false>);
+    ALLOW(plane::k_zpass16<true>);
 #undef ALLOW
     return cudaSuccess;
 }
@@ -582,7 +589,7 @@ cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
         Geometry g{plane::N, plane::N, plane::N, (long long)plane::N * plane::N * plane::N};
         return launch_tensor_zpass(s, X, g, t);
     }
-    plane::k_zpass16<<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
+    plane::k_zpass16<false><<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
         X, t.twx, t, plane::N, (long long)plane::N * plane::N);
     return cudaGetLastError();
 }
@@ -591,7 +598,7 @@ bool zpass256_supported(const Geometry& g) { return g.nzb == plane::N && g.nxb %
 
 cudaError_t launch_zpass256(cudaStream_t s, float2* X, const Geometry& g, const Tables& t)
 {
-    plane::k_zpass16<<<dim3(g.nxb / plane::ZW, g.nyb), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
+    plane::k_zpass16<true><<<dim3(g.nxb / plane::ZW, g.nyb), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
         X, t.twz, t, g.nxb, (long long)g.nxb * g.nyb);
     return cudaGetLastError();
 }
