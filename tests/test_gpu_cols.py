@@ -1,7 +1,9 @@
 """Register column transforms (ose_cols.cu, y and z passes of the generic path
 for lengths 16 C) against the FP64 oracle: one operator application on grids
 whose y and z lengths cover every compiled C (4, 6, 8, 9, 10, 11, 12, 16, 18,
-20, 23, 24).  Bound: 2e-6 relative L2 (FP32 transforms)."""
+20, 23, 24), and grids with 256 z planes, whose z pass is the 16-column
+256-point kernel with runtime strides.  Bound: 2e-6 relative L2 (FP32
+transforms)."""
 import numpy as np
 import pytest
 
@@ -12,7 +14,8 @@ from golden_util import rel_l2
 pytestmark = pytest.mark.gpu
 
 # padded (nxb, nyb, nzb); sponge 4 on every side
-GRIDS = [(48, 64, 96), (40, 144, 176), (24, 160, 192), (16, 288, 320), (16, 368, 384), (16, 256, 128)]
+GRIDS = [(48, 64, 96), (40, 144, 176), (24, 160, 192), (16, 288, 320), (16, 368, 384), (16, 256, 128),
+         (64, 96, 256), (32, 48, 256)]
 
 
 @pytest.fixture(scope="module", autouse=True)
