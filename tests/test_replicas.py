@@ -1,7 +1,8 @@
-"""The N-GPU form of the bench is replicas only: one independent shot per
-rank, no data-path collective; the ranks meet at a barrier around the timed
-region and the slowest rank's time sets the whole-job rate.  World size 2 on
-the gloo backend (CPU), rendezvous on 127.0.0.1."""
+"""The N-GPU forms of the bench have no data-path collective: replicas (one
+independent shot per rank) for the single-shot step, and the batched form's
+shots dealt round-robin to the ranks.  The ranks meet at a barrier around the
+timed region and the slowest rank's time sets the whole-job rate.  World size
+2 on the gloo backend (CPU), rendezvous on 127.0.0.1."""
 import os
 import socket
 import sys
@@ -30,9 +31,11 @@ def _rank_main(rank, world, port, q):
     ms = 100.0 + 25.0 * r            # the ranks' own step times differ
     ms_max = d.max(ms)
     rate = bench.replica_rate(w, 256 ** 3, 300, ms_max)
+    shots = bench.shard(range(64), r, w)    # the batched form's shots on this rank
+    total = d.sum(float(len(shots)))
     d.barrier()
     d.close()
-    q.put((r, w, local, ms_max, rate))
+    q.put((r, w, local, ms_max, rate, shots, total))
 
 
 def test_two_replicas_meet_and_take_the_slowest_rank():
@@ -51,6 +54,9 @@ def test_two_replicas_meet_and_take_the_slowest_rank():
     assert all(o[3] == 125.0 for o in out)                       # max over ranks, seen by both
     expect = 2 * 256 ** 3 * 300 / 0.125 / 1e9                   # whole job: both replicas' cells
     assert all(abs(o[4] - expect) < 1e-9 * expect for o in out)
+    # batched shots: disjoint round-robin shares covering all 64, counted once
+    assert sorted(out[0][5] + out[1][5]) == list(range(64)) and not set(out[0][5]) & set(out[1][5])
+    assert all(o[6] == 64.0 for o in out)
 
 
 def test_single_rank_needs_no_process_group():
