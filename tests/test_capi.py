@@ -76,3 +76,32 @@ def test_python_class_mirrors_header_structs():
 def test_corrector_param_count_matches_the_restatement(lib):
     import corrector_torch as CT
     assert ose3d.corrector_param_count() == CT.param_count() == 64034
+
+
+def _create(lib, p, vel):
+    h = ctypes.c_void_p()
+    st = lib.ose_create(ctypes.byref(p), vel.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(h))
+    return st, h
+
+
+@pytest.mark.parametrize("case", ["axis_too_long", "receivers_below_model", "zero_velocity", "nan_velocity"])
+def test_create_rejects_before_touching_the_device(lib, case):
+    """ose_create validates sizes, geometry and the model on the host first,
+    so these refusals need no GPU (and allocate nothing)."""
+    kw = dict(nx=12, ny=10, nz=8, bu=4, bd=4, bl=4, br=4, bf=4, bb=4, nt=10, sxbeg=5, sybeg=5, szbeg=2)
+    if case == "axis_too_long":
+        kw.update(nx=1030 - 8)                      # padded 1030 > 1024
+    if case == "receivers_below_model":
+        kw.update(gzbeg=8)                          # depth index past the interior
+    p = ose3d.default_params(**kw)
+    vel = np.full((kw["nx"], kw["ny"], kw["nz"]), 2000.0, np.float32)
+    if case == "zero_velocity":
+        vel[3, 4, 5] = 0.0
+    if case == "nan_velocity":
+        vel[0, 0, 0] = np.nan
+    st, h = _create(lib, p, vel)
+    assert not h.value
+    expect = {"axis_too_long": (5, b"1024"), "receivers_below_model": (1, b"gzbeg"),
+              "zero_velocity": (1, b"positive"), "nan_velocity": (1, b"finite")}[case]
+    assert st == expect[0]
+    assert expect[1] in lib.ose_last_error(None)
