@@ -62,7 +62,8 @@ def test_time_loop_matches_reference_goldens(name):
         assert abs(np.linalg.norm(Q.astype(np.float64)) / g["Q_norm"] - 1) < TOL
 
 
-@pytest.mark.parametrize("dims", [(20, 18, 16, 6), (9, 13, 11, 5), (40, 24, 30, 8)])
+# the last case: the longest padded axis the transforms take (1024 in x)
+@pytest.mark.parametrize("dims", [(20, 18, 16, 6), (9, 13, 11, 5), (40, 24, 30, 8), (1016, 8, 8, 4)])
 def test_operator_matches_oracle(dims):
     nx, ny, nz, b = dims
     rng = np.random.default_rng(nx * 100 + ny)
