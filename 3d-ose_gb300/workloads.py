@@ -66,6 +66,11 @@ CONFIGS = {
                dict(nx=101, ny=101, nz=101, bu=20, bd=20, bl=20, br=20, bf=20, bb=20, nt=1000,
                     fm=20.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
                     sxbeg=50, sybeg=50, szbeg=10, gzbeg=5)),
+    # the same with the Cerjan sponge, factor 0.015
+    "ose142cerjan": (lambda: layered_perturbed(101, 101, 101),
+                     dict(nx=101, ny=101, nz=101, bu=20, bd=20, bl=20, br=20, bf=20, bb=20, nt=1000,
+                          fm=20.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                          sxbeg=50, sybeg=50, szbeg=10, gzbeg=5, sponge_mode=1, cerjan_factor=0.015)),
 }
 
 

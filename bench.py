@@ -413,8 +413,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="learned workload: timing only")
     ap.add_argument("--workload", default=WORKLOAD,
-                    choices=[WORKLOAD, "ose320x288x256", "ose384x384x256", "ose142", "batched64", "precision",
-                             "learned"])
+                    choices=[WORKLOAD, "ose320x288x256", "ose384x384x256", "ose142", "ose142cerjan", "batched64",
+                             "precision", "learned"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
