@@ -61,6 +61,34 @@ __device__ void fft_stage(const float2* __restrict__ in, float2* __restrict__ ou
     const int m = n / r;
     const int tstep = n / (p * r);
     const int total = L * m;
+    if (r > 4) {
+        // radix 5, 7 and larger primes: one output q of one butterfly per work
+        // item, y_q = sum_j x_j W_n^(j te) W_r^(j q), the two exponents
+        // combined into one table index e_j = j te + (j q mod r) n / r < 2n
+        const int nr = n / r;
+        for (int b = threadIdx.x; b < total * r; b += blockDim.x) {
+            const int q = b % r, bb = b / r;
+            int l, i;
+            if (line_fastest) { l = bb % L; i = bb / L; }
+            else { l = bb / m; i = bb - l * m; }
+            const int k = i % p;
+            const int te = k * tstep;
+            const float2* src = in + l * LS + i * ES;
+            const int ms = m * ES;
+            float2 acc = make_float2(0.f, 0.f);
+            int jte = 0, jq = 0;
+            for (int j = 0; j < r; ++j) {
+                int e = jte + jq * nr;
+                if (e >= n) e -= n;
+                acc = cadd(acc, cmul(src[j * ms], twiddle<INV>(tw, e)));
+                jte += te;
+                jq += q;
+                if (jq >= r) jq -= r;
+            }
+            out[l * LS + ((i - k) * r + k + q * p) * ES] = acc;
+        }
+        return;
+    }
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
         int l, i;
         if (line_fastest) { l = b % L; i = b / L; }
@@ -101,17 +129,6 @@ __device__ void fft_stage(const float2* __restrict__ in, float2* __restrict__ ou
             dst[0] = cadd(x0, s);
             dst[ps] = cadd(t, ihd);
             dst[2 * ps] = csub(t, ihd);
-        } else {
-            const int nr = n / r;
-            for (int q = 0; q < r; ++q) {
-                float2 acc = make_float2(0.f, 0.f);
-                for (int j = 0; j < r; ++j) {
-                    float2 x = src[j * ms];
-                    if (te) x = cmul(x, twiddle<INV>(tw, j * te));
-                    acc = cadd(acc, cmul(x, twiddle<INV>(tw, ((j * q) % r) * nr)));
-                }
-                dst[q * ps] = acc;
-            }
         }
     }
 }

@@ -62,8 +62,10 @@ def test_time_loop_matches_reference_goldens(name):
         assert abs(np.linalg.norm(Q.astype(np.float64)) / g["Q_norm"] - 1) < TOL
 
 
-# the last case: the longest padded axis the transforms take (1024 in x)
-@pytest.mark.parametrize("dims", [(20, 18, 16, 6), (9, 13, 11, 5), (40, 24, 30, 8), (1016, 8, 8, 4)])
+# (1016, 8, 8, 4): the longest padded axis the transforms take (1024 in x);
+# (61, 134, 8, 4): padded 70 = 2 5 7 and 142 = 2 71 (the direct-DFT radices)
+@pytest.mark.parametrize("dims", [(20, 18, 16, 6), (9, 13, 11, 5), (40, 24, 30, 8), (1016, 8, 8, 4),
+                                  (61, 134, 8, 4)])
 def test_operator_matches_oracle(dims):
     nx, ny, nz, b = dims
     rng = np.random.default_rng(nx * 100 + ny)
