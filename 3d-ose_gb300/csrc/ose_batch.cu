@@ -216,11 +216,8 @@ cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
     ea.az = D.az;
     ea.S = D.S;
     ea.wout = D.W;
-    ea.w = D.W;
     ea.sch = D.sch;
     ea.scl = D.scl;
-    ea.c0 = D.c0;
-    ea.c0l = D.c0l;
     ea.gather = D.gather;
     ea.cur = D.ctr + 1;
     ea.gz = D.gz;
@@ -235,6 +232,9 @@ cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
         ea.prev = n == 0 ? D.A : ((n & 1) ? D.W : D.A);
         ea.c1 = D.c[n];
         ea.c1l = D.cl[n];
+        ea.cp = n == 1 ? D.c0 : (n >= 2 ? D.c[n - 2] : 0.f);
+        ea.cpl = n == 1 ? D.c0l : (n >= 2 ? D.cl[n - 2] : 0.f);
+        ea.sp = ose::sum_plan(n, D.M);
         const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == D.M ? ose::EPI_LAST : ose::EPI_MID);
         e = ose::launch_generic_application(st, D.g, D.px, D.py, D.pz, t, an, D.X, mode, ea, nullptr,
                                             fuse && n > 0, fuse && n < D.M);

@@ -245,25 +245,12 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm, bool source
     for (int n = 0; n <= M; ++n) {
         e = timed(tm, s, 1, 16.0 * N, [&] { return ose::launch_zpass(s, h->X, h->tables); });
         if (e != cudaSuccess) return e;
-        ose::EpiMode mode;
-        double bytes;
-        int cls;
-        if (n == 0) {
-            ea.prev = h->A;
-            ea.w = h->W;
-            ose::split_float(h->J[0], &ea.c0, &ea.c0l);
-            ose::split_float(2.0 * h->J[1], &ea.c1, &ea.c1l);
-            mode = ose::EPI_FIRST;
-            bytes = (M > 0 ? 44.0 : 36.0) * N;
-            cls = 2;
-        } else {
-            ea.prev = (n & 1) ? h->W : h->A;
-            ose::split_float(2.0 * h->J[n + 1], &ea.c1, &ea.c1l);
-            mode = n == M ? ose::EPI_LAST : ose::EPI_MID;
-            bytes = (n == M ? 36.0 : 52.0) * N;
-            cls = n == M ? 4 : 3;
-        }
+        const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == M ? ose::EPI_LAST : ose::EPI_MID);
+        ea.prev = n == 0 ? h->A : ((n & 1) ? h->W : h->A);
+        ose::set_application(ea, n, M, h->J.data());
         const bool fwd = n < M;
+        const double bytes = ose::epilogue_bytes(mode, ea.sp, fwd) * N;
+        const int cls = mode == ose::EPI_FIRST ? 2 : (mode == ose::EPI_LAST ? 4 : (ea.sp.touch ? 3 : 8));
         e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->tables, ea); });
         if (e != cudaSuccess) return e;
     }
@@ -299,30 +286,22 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = tru
     ea.ny = h->p.ny;
     ea.nt = h->p.nt;
     const double N = (double)h->g.ncell;
-    // n = 0: a_1 = -i L a_0, S = J0 a_0 + 2 J1 a_1
-    ea.prev = h->A;
-    ea.w = h->W;
-    ose::split_float(h->J[0], &ea.c0, &ea.c0l);
-    ose::split_float(2.0 * h->J[1], &ea.c1, &ea.c1l);
     // with the register row kernels, the row pass of application n also
     // writes the x transform of a_{n+1}, so application n + 1 skips its x pass
     const bool fuse = ose::generic_fuses_x(h->px);
-    e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, h->W, h->X,
-                                        ose::EPI_FIRST, ea, tm, false, fuse && M > 0);
-    if (tm) {
-        for (int c = 0; c < 4; ++c) tm->bytes[c] += 16.0 * N;
-        tm->bytes[4] += (fuse && M > 0 ? 44.0 : 36.0) * N;
-    }
-    if (e != cudaSuccess) return e;
-    for (int n = 1; n <= M; ++n) {
-        const float2* an = (n & 1) ? h->A : h->W;
-        ea.prev = (n & 1) ? h->W : h->A;
-        ose::split_float(2.0 * h->J[n + 1], &ea.c1, &ea.c1l);
-        e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, an, h->X,
-                                            n == M ? ose::EPI_LAST : ose::EPI_MID, ea, tm, fuse, fuse && n < M);
+    for (int n = 0; n <= M; ++n) {
+        // n = 0: a_1 = -i L a_0 from a_0 = W
+        const float2* an = n == 0 ? h->W : ((n & 1) ? h->A : h->W);
+        const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == M ? ose::EPI_LAST : ose::EPI_MID);
+        ea.prev = n == 0 ? h->A : ((n & 1) ? h->W : h->A);
+        ose::set_application(ea, n, M, h->J.data());
+        const bool fwd = fuse && n < M;
+        e = ose::launch_generic_application(h->stream, h->g, h->px, h->py, h->pz, h->tables, an, h->X, mode, ea,
+                                            tm, fuse && n > 0, fwd);
         if (tm) {
-            for (int c = fuse ? 1 : 0; c < 4; ++c) tm->bytes[c] += 16.0 * N;
-            tm->bytes[4] += (n == M ? 36.0 : (fuse ? 52.0 : 44.0)) * N;
+            for (int c = (fuse && n > 0) ? 1 : 0; c < 4; ++c) tm->bytes[c] += 16.0 * N;
+            const bool skip = mode != ose::EPI_LAST && !ea.sp.touch;
+            tm->bytes[skip ? 8 : 4] += ose::epilogue_bytes(mode, ea.sp, fwd) * N;
         }
         if (e != cudaSuccess) return e;
     }
@@ -1204,25 +1183,33 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
     if (!h->shot_ready) return fail(h, OSE_ERR_STATE, "ose_reset_shot must come first");
     if (h->it + reps > h->p.nt) return fail(h, OSE_ERR_INVALID, "reps beyond nt");
     ose::KernelTiming& t = h->timing;
+    // class 8: the epilogue passes that leave the partial sum alone (SumPlan)
     static const char* kGeneric[] = {"fft_x_fwd", "fft_y_fwd", "fft_z_kscale", "fft_y_inv",
-                                     "fft_x_inv_epilogue", "inject", "corrector_scale", "corrector"};
+                                     "fft_x_inv_epilogue", "inject", "corrector_scale", "corrector",
+                                     "fft_x_inv_epilogue_nosum", "unused"};
     static const char* kPlane[] = {"plane_fwd", "zpass", "plane_inv_first", "plane_inv_mid",
-                                   "plane_inv_last", "inject", "corrector_scale", "corrector"};
+                                   "plane_inv_last", "inject", "corrector_scale", "corrector",
+                                   "plane_inv_mid_nosum", "unused"};
     const char** kNames = h->d.path == OSE_PATH_PLANE ? kPlane : kGeneric;
-    const int nc = h->corr ? 8 : 6;
     for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
     for (int r = 0; r < reps; ++r) {
         CK(h, enqueue_step(h, &t));
         CK(h, cudaStreamSynchronize(h->stream));
         h->it += 1;
     }
-    *count = nc;
-    for (int c = 0; c < nc && c < cap; ++c) {
-        if (names) names[c] = kNames[c];
-        if (ms) ms[c] = t.count[c] ? t.ms[c] / t.count[c] : 0.f;
-        if (bytes) bytes[c] = t.count[c] ? t.bytes[c] / t.count[c] : 0.0;
-        if (launches) launches[c] = t.count[c] / reps;
+    // the classes that launched (inject always, the corrector when set)
+    int nc = 0;
+    for (int c = 0; c < ose::KernelTiming::kClasses; ++c) {
+        if (!t.count[c] && c != 5) continue;
+        if (nc < cap) {
+            if (names) names[nc] = kNames[c];
+            if (ms) ms[nc] = t.count[c] ? t.ms[c] / t.count[c] : 0.f;
+            if (bytes) bytes[nc] = t.count[c] ? t.bytes[c] / t.count[c] : 0.0;
+            if (launches) launches[nc] = t.count[c] / reps;
+        }
+        ++nc;
     }
+    *count = nc;
     return OSE_OK;
 }
 

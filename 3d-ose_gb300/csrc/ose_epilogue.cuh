@@ -15,6 +15,30 @@ namespace ose {
 // next application's forward x transform of the new term.
 enum { EPI_NONE = -1, EPI_SCALE_VEL = 4, EPI_FIRST_FWD = 5, EPI_MID_FWD = 6 };
 
+// The partial-sum update of one cell at a FIRST/MID/LAST application, by the
+// schedule e.sp (SumPlan): s = the stored S (zero unless e.sp.s_read),
+// am = a_{n-1}, an = a_{n+1}, att = the cell's sponge factor.  Branch-free:
+// the powers att^k (k <= kSumMaxPow) are selected, absent terms get factor 0.
+__device__ __forceinline__ float2 sum_update(const EpiArgs& e, float att, float2 s, float2 am, float2 an)
+{
+    const SumPlan& p = e.sp;
+    const float a2 = att * att, a3 = a2 * att;
+    auto pw = [&](int k) { return k == 0 ? 1.f : (k == 1 ? att : (k == 2 ? a2 : a3)); };
+    const float fS = p.s_read ? pw(p.kS) : 0.f;
+    const float gP = p.add_prev ? pw(p.kP) : 0.f;
+    const float gN = p.add_new ? pw(p.kN) : 0.f;
+    const float fP = e.cp * gP, fN = e.c1 * gN;
+    float2 r = make_float2(s.x * fS, s.y * fS);
+    if (kCompensatedConstants) {
+        const float lP = e.cpl * gP, lN = e.c1l * gN;
+        r.x = fmaf(lP, am.x, fmaf(lN, an.x, r.x));
+        r.y = fmaf(lP, am.y, fmaf(lN, an.y, r.y));
+    }
+    r.x = fmaf(fP, am.x, fmaf(fN, an.x, r.x));
+    r.y = fmaf(fP, am.y, fmaf(fN, an.y, r.y));
+    return r;
+}
+
 // The pointwise work of one application on cell i = (x, y, z); X is the
 // unnormalised inverse transform, e.vs the velocity, (e.sch + e.scl) = 1/(R N).
 template <int EPI>
@@ -28,27 +52,21 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
     if (EPI == EPI_SCALE || EPI == EPI_SCALE_VEL) {
         e.prev[i] = Lx;
     } else if (EPI == EPI_FIRST) {
-        // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1   (ose_3d_lib.cu:651-744)
+        // a_1 = -i L a_0   (ose_3d_lib.cu:651-731); S by the schedule
         const float2 a1 = make_float2(Lx.y, -Lx.x);
-        const float2 w = e.w[i];
         e.prev[i] = a1;
-        if (kCompensatedConstants)
-            e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
-                                 fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
-        else
-            e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+        if (e.sp.touch) e.S[i] = sum_update(e, 1.f, make_float2(0.f, 0.f), a1, a1);
     } else {
-        // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att   (ose_3d_lib.cu:750-870)
+        // a_{n+1} = a_{n-1} - 2i L a_n   (ose_3d_lib.cu:750-833); the partial
+        // sum and sponge of ose_3d_lib.cu:839-860 by the schedule
         const float2 am = e.prev[i];
         const float2 an = make_float2(fmaf(2.f, Lx.y, am.x), fmaf(-2.f, Lx.x, am.y));
-        const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
-        float2 s = e.S[i];
-        if (kCompensatedConstants) {
-            s.x = fmaf(e.c1l, an.x, s.x);
-            s.y = fmaf(e.c1l, an.y, s.y);
+        if (EPI == EPI_MID && !e.sp.touch) {
+            e.prev[i] = an;
+            return;
         }
-        s.x = fmaf(e.c1, an.x, s.x) * att;
-        s.y = fmaf(e.c1, an.y, s.y) * att;
+        const float att = __ldg(e.ax + x) * __ldg(e.ay + y) * __ldg(e.az + z);
+        const float2 s = sum_update(e, att, e.sp.s_read ? e.S[i] : make_float2(0.f, 0.f), am, an);
         if (EPI == EPI_MID) {
             e.prev[i] = an;
             e.S[i] = s;
@@ -85,15 +103,14 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
             const int k = CH * h + q;
             const long long i = i0 + (long long)k * xs;
             vv[q] = __ldg(e.vs + i);
-            if (EPI == EPI_FIRST) am[q] = e.w[i];
             if (EPI == EPI_MID || EPI == EPI_LAST) {
                 am[q] = e.prev[i];
-                sm[q] = e.S[i];
-                axv[q] = __ldg(e.ax + x0 + k * xs);
+                sm[q] = e.sp.s_read ? e.S[i] : make_float2(0.f, 0.f);
+                axv[q] = e.sp.touch ? __ldg(e.ax + x0 + k * xs) : 1.f;
             }
         }
         float ayz0 = 0.f, ayz1 = 0.f;
-        if (EPI == EPI_MID || EPI == EPI_LAST) {
+        if ((EPI == EPI_MID || EPI == EPI_LAST) && e.sp.touch) {
             ayz0 = __ldg(e.ay + y);
             ayz1 = __ldg(e.az + z);
         }
@@ -110,29 +127,17 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
                 e.prev[i] = Lx;
             } else if (EPI == EPI_FIRST) {
                 const float2 a1 = make_float2(Lx.y, -Lx.x);
-                const float2 w = am[q];
                 e.prev[i] = a1;
-                if (kCompensatedConstants)
-                    e.S[i] = make_float2(fmaf(e.c0, w.x, fmaf(e.c1, a1.x, fmaf(e.c0l, w.x, e.c1l * a1.x))),
-                                         fmaf(e.c0, w.y, fmaf(e.c1, a1.y, fmaf(e.c0l, w.y, e.c1l * a1.y))));
-                else
-                    e.S[i] = make_float2(fmaf(e.c0, w.x, e.c1 * a1.x), fmaf(e.c0, w.y, e.c1 * a1.y));
+                if (e.sp.touch) e.S[i] = sum_update(e, 1.f, make_float2(0.f, 0.f), a1, a1);
                 if (KEEP) v[k] = a1;
             } else {
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
-                const float att = axv[q] * ayz0 * ayz1;
-                float2 s = sm[q];
-                if (kCompensatedConstants) {
-                    s.x = fmaf(e.c1l, an.x, s.x);
-                    s.y = fmaf(e.c1l, an.y, s.y);
-                }
-                s.x = fmaf(e.c1, an.x, s.x) * att;
-                s.y = fmaf(e.c1, an.y, s.y) * att;
                 if (EPI == EPI_MID) {
                     e.prev[i] = an;
-                    e.S[i] = s;
+                    if (e.sp.touch) e.S[i] = sum_update(e, axv[q] * ayz0 * ayz1, sm[q], am[q], an);
                     if (KEEP) v[k] = an;
                 } else {
+                    const float2 s = sum_update(e, axv[q] * ayz0 * ayz1, sm[q], am[q], an);
                     e.wout[i] = s;
                     if (z == e.gz) {
                         const int ix = x - e.bl, iy = y - e.bf;
@@ -157,14 +162,14 @@ __device__ __forceinline__ EpiArgs batch_epi(const BatchShot& S, int n)
     e.az = S.az;
     e.S = S.S;
     e.wout = S.W;
-    e.w = S.W;
     e.prev = n == 0 ? S.A : ((n & 1) ? S.W : S.A);
     e.sch = S.sch;
     e.scl = S.scl;
-    e.c0 = S.c0;
-    e.c0l = S.c0l;
     e.c1 = S.c[n];
     e.c1l = S.cl[n];
+    e.cp = n == 1 ? S.c0 : (n >= 2 ? S.c[n - 2] : 0.f);
+    e.cpl = n == 1 ? S.c0l : (n >= 2 ? S.cl[n - 2] : 0.f);
+    e.sp = sum_plan(n, S.M);
     e.gather = S.gather;
     e.cur = S.ctr + 1;
     e.gz = S.gz;

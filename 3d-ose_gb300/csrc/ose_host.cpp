@@ -166,7 +166,8 @@ void hilbert_trace(const std::vector<float>& w, int div_nt, std::vector<float>& 
     });
 }
 
-// Radix plan: 4s first, then 2, 3, 5, 7 and any remaining prime.
+// Radix plan: a prime factor >= 11 (when the length has one, taken once), then
+// 4s, 2, 3, 5, 7 and any remaining prime.
 int plan_axis(int n, AxisPlan* p)
 {
     memset(p, 0, sizeof(*p));
@@ -178,6 +179,16 @@ int plan_axis(int n, AxisPlan* p)
         p->radix[p->ns++] = r;
         return true;
     };
+    // a prime factor >= 11 goes first: the first stage has no input twiddles,
+    // which the paired direct DFT of ose_kernels.cu needs
+    int big = 0;
+    {
+        int t = m;
+        for (int f = 2; f * f <= t; ++f)
+            while (t % f == 0) t /= f;   // t = the largest prime factor
+        if (t >= 11) big = t;
+    }
+    if (big) { if (!push(big)) return -1; m /= big; }
     while (m % 4 == 0) { if (!push(4)) return -1; m /= 4; }
     while (m % 2 == 0) { if (!push(2)) return -1; m /= 2; }
     for (int f = 3; m > 1; f += 2) {

@@ -31,9 +31,63 @@ struct Geometry {
 // (wavefield_extro_ori2, ose_3d_lib.cu:651-870, fused).
 enum EpiMode { EPI_FIRST = 0, EPI_MID = 1, EPI_LAST = 2, EPI_SCALE = 3 };
 
+// Schedule of the Chebyshev partial sum S over the applications of one step.
+// The reference adds a_{n+1} to S at application n and multiplies S by the
+// sponge att after every addition (ose_3d_lib.cu:736-744, 839-860), so after
+// application n the term a_j carries att^e(j, n), e = n for j <= 1 and
+// n - j + 2 for j >= 2, and the new state is S after application M.  Here
+// every term a_j is added exactly once, at an application where the epilogue
+// holds it anyway: application j - 1 (it is the new term a_{n+1}) or j + 1
+// (it is a_{n-1}, read for the recurrence), with the power of att it carries
+// there; S itself is multiplied by att^(n - n') where n' is the application
+// that last stored it.  Terms are taken in pairs (a_{4k}, a_{4k+2}) at
+// application 4k + 1 and (a_{4k+1}, a_{4k+3}) at 4k + 2, so S is read and
+// written at 6 of the 11 applications of M = 10 instead of at all of them
+// (the other applications write only the recurrence term), and the first
+// application reads neither the state nor S.  Same sum, same sponge powers;
+// only the rounding order differs.
+struct SumPlan {
+    int add_prev;   // add c_{n-1} att^kP a_{n-1}
+    int add_new;    // add c_{n+1} att^kN a_{n+1}
+    int s_read;     // S holds earlier terms (else this application starts it)
+    int touch;      // S is updated here (MID: S written; LAST: always, writes the state)
+    int kS, kP, kN; // powers of att on the stored S, a_{n-1} and a_{n+1}
+};
+
+// Application at which term a_j (j = 0 .. M + 1) is added.
+__host__ __device__ inline int sum_term_app(int j, int M)
+{
+    if ((j & 3) < 2) return j + 1 <= M ? j + 1 : j - 1;
+    return j - 1;
+}
+
+__host__ __device__ inline bool sum_touches(int n, int M)
+{
+    return n == M || sum_term_app(n + 1, M) == n || (n >= 1 && sum_term_app(n - 1, M) == n);
+}
+
+__host__ __device__ inline SumPlan sum_plan(int n, int M)
+{
+    SumPlan p{};
+    p.add_prev = n >= 1 && sum_term_app(n - 1, M) == n;
+    p.add_new = sum_term_app(n + 1, M) == n;
+    p.touch = sum_touches(n, M);
+    int last = -1;
+    for (int k = n - 1; k >= 0; --k)
+        if (sum_touches(k, M)) { last = k; break; }
+    p.s_read = p.touch && last >= 0;
+    p.kS = p.s_read ? n - last : 0;
+    const int jp = n - 1, jn = n + 1;
+    p.kP = jp <= 1 ? n : n - jp + 2;
+    p.kN = jn <= 1 ? n : n - jn + 2;
+    return p;
+}
+
+// The powers a SumPlan uses are 0 .. 3 for every series order M.
+constexpr int kSumMaxPow = 3;
+
 struct EpiArgs {
     float2* prev;         // FIRST: a_1 out.  MID/LAST: a_{n-1} in, a_{n+1} out (MID)
-    const float2* w;      // FIRST: a_0 = W
     float2* S;            // partial sum
     float2* wout;         // LAST: new state (P, Q)
     const float* vs;      // velocity v per cell (the model value itself)
@@ -42,8 +96,9 @@ struct EpiArgs {
     const float* az;      // sponge, z
     // Constants as unevaluated float pairs hi + lo (about 48 significant
     // bits), so that no rounded constant biases every step the same way:
-    float c0, c0l;        // FIRST: J0
-    float c1, c1l;        // FIRST: 2 J1.  MID/LAST: 2 J_{n+1}
+    float c1, c1l;        // coefficient of the new term a_{n+1}: 2 J_{n+1}
+    float cp, cpl;        // coefficient of a_{n-1}: J0 (n = 1) or 2 J_{n-1}
+    SumPlan sp;           // what this application adds to S
     float sch, scl;       // 1 / (R N), the scale of v * IFFT3(|k| FFT3(.))
     // receivers (LAST)
     float* gather;        // [nt][ng]
@@ -77,11 +132,39 @@ struct Tables {
 // 1.86e-4) and cost about 6% of the step, so they are off.
 constexpr bool kCompensatedConstants = false;
 
+// Twiddles as float pairs (hi + lo) in every 256-point transform of the plane
+// kernels (ose_plane.cu, k_zpass16 included).  Off: the measured 2000-step
+// error of the 256^3 workload is the same either way (round-off, not twiddle
+// bias, dominates) and the pairs cost about 8% of the step.
+constexpr bool kCompensatedTwiddles = false;
+
 // hi + lo split of a double: hi = nearest float, lo = nearest float to the rest.
 inline void split_float(double v, float* hi, float* lo)
 {
     *hi = (float)v;
     *lo = kCompensatedConstants ? (float)(v - (double)*hi) : 0.f;
+}
+
+// Coefficients and partial-sum schedule of application n of M + 1 (J = the
+// Bessel values J_0 .. J_{M+1} of the step, in double).
+inline void set_application(EpiArgs& e, int n, int M, const double* J)
+{
+    split_float(2.0 * J[n + 1], &e.c1, &e.c1l);
+    split_float(n == 1 ? J[0] : (n >= 2 ? 2.0 * J[n - 1] : 0.0), &e.cp, &e.cpl);
+    e.sp = sum_plan(n, M);
+}
+
+// HBM bytes per cell of the epilogue of application n (FIRST, MID, LAST):
+// reads X, v and (MID, LAST) a_{n-1}; writes the new term (or, LAST, the
+// state); S read and written as the schedule says; fwd: the fused forward
+// transform of the new term also writes X.
+inline double epilogue_bytes(EpiMode mode, const SumPlan& sp, bool fwd)
+{
+    double b = 8.0 + 4.0 + 8.0 + (fwd ? 8.0 : 0.0);
+    if (mode != EPI_FIRST) b += 8.0;
+    if (sp.s_read) b += 8.0;
+    if (sp.touch && mode != EPI_LAST) b += 8.0;
+    return b;
 }
 
 // Host-side launch helpers (ose_kernels.cu).
@@ -190,7 +273,7 @@ size_t batch_lines_smem(int n, int tx);
 
 // Per-kernel-class timing used by ose_profile_step.
 struct KernelTiming {
-    static constexpr int kClasses = 8;
+    static constexpr int kClasses = 10;
     cudaEvent_t ev[2];
     float ms[kClasses];
     int count[kClasses];

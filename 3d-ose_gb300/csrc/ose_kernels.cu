@@ -61,6 +61,48 @@ __device__ void fft_stage(const float2* __restrict__ in, float2* __restrict__ ou
     const int m = n / r;
     const int tstep = n / (p * r);
     const int total = L * m;
+    if (r > 4 && p == 1 && (r & 1)) {
+        // odd radix r >= 5 as the first stage (no input twiddles): the paired
+        // direct DFT.  With s_j = x_j + x_{r-j}, d_j = x_j - x_{r-j} and
+        // W_r^(j q) = c - i s, for q = 1 .. (r-1)/2
+        //   y_q, y_{r-q} = x_0 + sum_j s_j c  -/+ i sum_j d_j s
+        // (signs swapped for the inverse), so one work item computes two
+        // outputs from (r-1)/2 terms: a quarter of the multiply-adds of the
+        // direct sum.  Item q = 0 computes y_0 = x_0 + sum_j s_j.
+        const int h = (r - 1) / 2, nr = n / r;
+        for (int b = threadIdx.x; b < total * (h + 1); b += blockDim.x) {
+            const int q = b % (h + 1), bb = b / (h + 1);
+            int l, i;
+            if (line_fastest) { l = bb % L; i = bb / L; }
+            else { l = bb / m; i = bb - l * m; }
+            const float2* src = in + l * LS + i * ES;
+            const int ms = m * ES;
+            const float2 x0 = src[0];
+            float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+            int jq = 0;
+            for (int j = 1; j <= h; ++j) {
+                jq += q;
+                if (jq >= r) jq -= r;
+                const float2 xa = src[j * ms], xb = src[(r - j) * ms];
+                const float2 w = tw[jq * nr];   // (cos, -sin) of 2 pi j q / r
+                A.x = fmaf(xa.x + xb.x, w.x, A.x);
+                A.y = fmaf(xa.y + xb.y, w.x, A.y);
+                B.x = fmaf(xa.x - xb.x, w.y, B.x);
+                B.y = fmaf(xa.y - xb.y, w.y, B.y);
+            }
+            // forward: y_q = x0 + A + i B, y_{r-q} = x0 + A - i B; inverse swapped
+            const float2 base = make_float2(x0.x + A.x, x0.y + A.y);
+            const float2 iB = INV ? make_float2(B.y, -B.x) : make_float2(-B.y, B.x);
+            float2* dst = out + l * LS + i * r * ES;
+            if (q == 0) {
+                dst[0] = base;
+            } else {
+                dst[q * ES] = cadd(base, iB);
+                dst[(r - q) * ES] = csub(base, iB);
+            }
+        }
+        return;
+    }
     if (r > 4) {
         // radix 5, 7 and larger primes: one output q of one butterfly per work
         // item, y_q = sum_j x_j W_n^(j te) W_r^(j q), the two exponents
@@ -287,6 +329,7 @@ cudaError_t configure_kernels()
     ALLOW((k_rows<true, EPI_MID>));
     ALLOW((k_rows<true, EPI_LAST>));
     ALLOW((k_rows<true, EPI_SCALE>));
+    ALLOW((k_rows<true, EPI_SCALE_VEL>));
     ALLOW((k_lines<false, false>));
     ALLOW((k_lines<true, false>));
     ALLOW((k_lines<false, true>));
@@ -295,7 +338,8 @@ cudaError_t configure_kernels()
 }
 
 // Timing classes of the generic path.
-enum { T_XF = 0, T_YF = 1, T_ZK = 2, T_YI = 3, T_XI = 4, T_INJ = 5 };
+// T_XI_NOSUM: the x inverse + epilogue passes that leave the partial sum alone.
+enum { T_XF = 0, T_YF = 1, T_ZK = 2, T_YI = 3, T_XI = 4, T_INJ = 5, T_XI_NOSUM = 8 };
 
 // x_ready: X already holds the forward x transform of a_n (written by the
 // previous application's fused row pass), so pass 1 is skipped.
@@ -378,7 +422,7 @@ cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const 
     const long long nrows = (long long)g.nyb * g.nzb;
     const int rpc = rows_per_cta(px.n);
     const unsigned nb = (unsigned)((nrows + rpc - 1) / rpc);
-    Timer T(tm, s, T_XI);
+    Timer T(tm, s, (mode != EPI_LAST && !e.sp.touch) ? T_XI_NOSUM : T_XI);
     if (fuse) {
         int epi = (int)mode;
         if (fwd_next && mode == EPI_FIRST) epi = EPI_FIRST_FWD;

@@ -37,6 +37,11 @@ cudaError_t launch_apply_operator_vel(cudaStream_t s, const Geometry& g, const A
 
 namespace {
 
+// The tables below hold single-float twiddles and squared wavenumbers only:
+// the low halves that the compensated variants read are not kept in the array.
+static_assert(!kCompensatedConstants && !kCompensatedTwiddles,
+              "the allocation-free entry point keeps no low-part tables");
+
 constexpr long long kMaxCells = OSE_NOALLOC_MAX_CELLS;
 constexpr int kMaxAxisLen = 1024;
 // layout of the array, in float2 units: scratch field | twiddles x, y, z | k^2 x, y, z
@@ -91,7 +96,8 @@ extern "C" ose_status ose_apply_operator_noalloc(int nxb, int nyb, int nzb, floa
         if (!g_addr[dev]) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return OSE_ERR_CUDA;
-            if (configure_kernels() != cudaSuccess) return OSE_ERR_CUDA;
+            if (configure_kernels() != cudaSuccess || configure_plane_kernels() != cudaSuccess)
+                return OSE_ERR_CUDA;
             g_addr[dev] = static_cast<float2*>(p);
         }
         base = g_addr[dev];

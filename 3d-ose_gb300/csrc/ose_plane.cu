@@ -22,8 +22,11 @@
 // memory connects the two radix-16 stages.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "ose_internal.h"
+#include "ose_epilogue.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -31,11 +34,7 @@ namespace ose {
 namespace plane {
 
 constexpr int N = 256;          // line length on all three axes
-// Twiddles as float pairs (hi + lo) in every 256-point transform.  Off: the
-// measured 2000-step error of the 256^3 workload is the same either way
-// (round-off, not twiddle bias, dominates) and the pairs cost about 8% of the
-// step; the Bessel coefficients, 1/(R N) and |k| stay compensated regardless.
-constexpr bool kCompensatedTwiddles = false;
+using ose::kCompensatedTwiddles;
 constexpr int CL = 8;           // CTAs per cluster (one plane per cluster)
 constexpr int SL = N / CL;      // rows / columns per CTA = 32
 // Line slots per thread: 2 (256 threads, up to 128 registers) or 1 (512
@@ -44,6 +43,10 @@ constexpr int NS = 2;
 constexpr int THREADS = 512 / NS;
 constexpr int WARPS = THREADS / 32;
 constexpr int ECH = NS == 1 ? 4 : 8;   // epilogue cells loaded ahead of their stores
+#ifndef OSE_PLANE_ECH_SUM
+#define OSE_PLANE_ECH_SUM 4
+#endif
+constexpr int ECH_SUM = OSE_PLANE_ECH_SUM;   // the same where S is read and written too
 constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
@@ -231,6 +234,15 @@ struct Args {
     EpiArgs e;
 };
 
+// Programmatic dependent launch.  The plane-path kernels are launched with
+// programmatic stream serialisation: the next kernel of the step may start
+// its CTAs (and load its constant tables) while the last wave of this one
+// runs; griddep_wait() then blocks until the previous kernel has completed
+// and its writes are visible, before anything it wrote is read.  Launched
+// without the attribute, both instructions do nothing.
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // W_256^t, t < 256, at tw[t] (nearest floats) and tw[256 + t] (remainders)
 __device__ __forceinline__ void load_twiddles(float2* tw, const float2* g, const float2* gl)
 {
@@ -296,6 +308,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
     load_twiddles(tw, a.tw, a.twl);
+    griddep_launch();
+    griddep_wait();
     float2 v0[16], v1[16];
     const float2* in = a.src + ((size_t)z * N + SL * r) * N;
 #pragma unroll
@@ -310,38 +324,39 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 }
 
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
-// recurrence, add_bessel_3d and apply_ABC_Xt of ose_3d_lib.cu:651-870, fused.
-// v holds the unnormalised inverse transform on entry and the new term a_{n+1}
-// (FIRST: a_1) on exit.  Loads are issued ECH cells at a time ahead of any
-// store; the buffers never overlap at different cells, so the restrict
-// qualifiers are exact.
-template <int EPI>
+// recurrence, and add_bessel_3d / apply_ABC_Xt of ose_3d_lib.cu:651-870 by
+// the partial-sum schedule e.sp (SumPlan), fused.  v holds the unnormalised
+// inverse transform on entry and the new term a_{n+1} (FIRST: a_1) on exit.
+// Loads are issued ECH cells at a time ahead of any store; the buffers never
+// overlap at different cells, so the restrict qualifiers are exact.
+// SUM (FIRST, MID): this application updates S (e.sp.touch); LAST always does.
+template <int EPI, bool SUM>
 __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e, int y, int z, int j)
 {
     float2* __restrict__ prev = e.prev;
     float2* __restrict__ S = e.S;
     float2* __restrict__ wout = e.wout;
-    const float2* __restrict__ w = e.w;
     const float* __restrict__ vs = e.vs;
     const size_t rowbase = ((size_t)z * N + y) * N + j;
-    const float attyz = (EPI == EPI_FIRST || EPI == EPI_SCALE) ? 1.f : __ldg(e.ay + y) * __ldg(e.az + z);
+    constexpr bool upd = EPI == EPI_LAST || (EPI == EPI_MID && SUM);
+    // cells whose loads are in flight together: fewer where S is read too
+    constexpr int CH = upd ? ECH_SUM : ECH;
+    const bool sread = upd && e.sp.s_read;
+    const float attyz = upd ? __ldg(e.ay + y) * __ldg(e.az + z) : 1.f;
 #pragma unroll
-    for (int h = 0; h < 16 / ECH; ++h) {
-        float vv[ECH];
-        float2 am[ECH], sm[ECH];
+    for (int h = 0; h < 16 / CH; ++h) {
+        float vv[CH];
+        float2 am[CH], sm[CH];
 #pragma unroll
-        for (int q = 0; q < ECH; ++q) {
-            const size_t i = rowbase + 16 * (ECH * h + q);
+        for (int q = 0; q < CH; ++q) {
+            const size_t i = rowbase + 16 * (CH * h + q);
             vv[q] = __ldg(vs + i);
-            if (EPI == EPI_FIRST) am[q] = w[i];
-            if (EPI == EPI_MID || EPI == EPI_LAST) {
-                am[q] = prev[i];
-                sm[q] = S[i];
-            }
+            if (EPI == EPI_MID || EPI == EPI_LAST) am[q] = prev[i];
+            sm[q] = sread ? S[i] : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int q = 0; q < ECH; ++q) {
-            const int n1 = ECH * h + q;
+        for (int q = 0; q < CH; ++q) {
+            const int n1 = CH * h + q;
             const int x = 16 * n1 + j;
             const size_t i = rowbase + 16 * n1;
             // L a_n = v * X * (sch + scl)  (vv = v / (R N) when not compensated)
@@ -351,31 +366,20 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
             if (EPI == EPI_SCALE) {
                 prev[i] = Lx;
             } else if (EPI == EPI_FIRST) {
-                // a_1 = -i L a_0 ; S = J0 a_0 + 2 J1 a_1
+                // a_1 = -i L a_0
                 const float2 a1 = make_float2(Lx.y, -Lx.x);
                 prev[i] = a1;
-                if (kCompensatedConstants)
-                    S[i] = make_float2(fmaf(e.c0, am[q].x, fmaf(e.c1, a1.x, fmaf(e.c0l, am[q].x, e.c1l * a1.x))),
-                                       fmaf(e.c0, am[q].y, fmaf(e.c1, a1.y, fmaf(e.c0l, am[q].y, e.c1l * a1.y))));
-                else
-                    S[i] = make_float2(fmaf(e.c0, am[q].x, e.c1 * a1.x), fmaf(e.c0, am[q].y, e.c1 * a1.y));
+                if (SUM) S[i] = sum_update(e, 1.f, make_float2(0.f, 0.f), a1, a1);
                 v[n1] = a1;
             } else {
-                // a_{n+1} = a_{n-1} - 2i L a_n ; S = (S + 2 J_{n+1} a_{n+1}) * att
+                // a_{n+1} = a_{n-1} - 2i L a_n
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
-                const float att = __ldg(e.ax + x) * attyz;
-                float2 s = sm[q];
-                if (kCompensatedConstants) {
-                    s.x = fmaf(e.c1l, an.x, s.x);
-                    s.y = fmaf(e.c1l, an.y, s.y);
-                }
-                s.x = fmaf(e.c1, an.x, s.x) * att;
-                s.y = fmaf(e.c1, an.y, s.y) * att;
                 if (EPI == EPI_MID) {
                     prev[i] = an;
-                    S[i] = s;
+                    if (upd) S[i] = sum_update(e, __ldg(e.ax + x) * attyz, sm[q], am[q], an);
                     v[n1] = an;
                 } else {
+                    const float2 s = sum_update(e, __ldg(e.ax + x) * attyz, sm[q], am[q], an);
                     wout[i] = s;
                     if (z == e.gz) {
                         const int ix = x - e.bl, iy = y - e.bf;
@@ -392,7 +396,7 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
 
 // Inverse y and x FFTs of plane z, the pointwise update, and (FWD) the
 // forward x and y FFTs of the new term.
-template <int EPI, bool FWD>
+template <int EPI, bool FWD, bool SUM = true>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane_inv(Args a)
 {
     extern __shared__ float4 smem4[];
@@ -402,18 +406,17 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
     // The epilogue's operands of this CTA's 32 rows are contiguous: start
-    // pulling them into L2 now, so the epilogue's loads hit L2.
-    if (threadIdx.x == 0 && EPI != EPI_SCALE) {
-        const size_t row0 = ((size_t)z * N + SL * r) * N;
-        prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
-        if (EPI == EPI_FIRST) {
-            prefetch_l2(a.e.w + row0, SL * N * sizeof(float2));
-        } else {
-            prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
-            prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
-        }
-    }
+    // pulling them into L2 now, so the epilogue's loads hit L2 (v is constant;
+    // a_{n-1} and S only once the kernels that wrote them have completed).
+    const size_t row0 = ((size_t)z * N + SL * r) * N;
+    if (threadIdx.x == 0 && EPI != EPI_SCALE) prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
     load_twiddles(tw, a.tw, a.twl);
+    griddep_launch();
+    griddep_wait();
+    if (threadIdx.x == 0 && EPI != EPI_SCALE && EPI != EPI_FIRST) {
+        prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
+        if (SUM && a.e.sp.s_read) prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
+    }
     float2 v0[16], v1[16];
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
     const float2* in = a.src + (size_t)z * N * N + SL * r;
@@ -452,8 +455,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     cluster.sync();
     fft256<true, true>(T, tw, v0, v1);
     // pointwise update on (x = 16 n1 + j, y, z)
-    epilogue_slot<EPI>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
-    if (NS > 1) epilogue_slot<EPI>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
+    epilogue_slot<EPI, SUM>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
+    if (NS > 1) epilogue_slot<EPI, SUM>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
     if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
@@ -487,6 +490,8 @@ __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X,
     float2* T = reinterpret_cast<float2*>(smem4);
     float2* tw = T + 16 * 16 * ZW;
     load_twiddles(tw, gtw, t.twl);
+    griddep_launch();
+    griddep_wait();
     const int c = threadIdx.x & (ZW - 1), j = threadIdx.x / ZW;
     const int ky = blockIdx.y, kx = ZW * blockIdx.x + c;
     const int nxb = GRID ? nxb_arg : N;
@@ -547,6 +552,35 @@ __global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X,
 
 }  // namespace plane
 
+// Programmatic stream serialisation for the plane-path launches (griddep_wait
+// in every kernel below keeps them ordered); OSE3D_PDL=0 turns it off.
+static bool pdl_enabled()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("OSE3D_PDL");
+        v = (e && strcmp(e, "0") == 0) ? 0 : 1;
+    }
+    return v == 1;
+}
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 bool plane_path_supported(int nxb, int nyb, int nzb)
 {
     return nxb == plane::N && nyb == plane::N && nzb == plane::N;
@@ -562,7 +596,10 @@ cudaError_t configure_plane_kernels()
         return e
     ALLOW(plane::k_plane_fwd);
     ALLOW((plane::k_plane_inv<EPI_FIRST, true>));
+    ALLOW((plane::k_plane_inv<EPI_FIRST, true, false>));
     ALLOW((plane::k_plane_inv<EPI_MID, true>));
+    ALLOW((plane::k_plane_inv<EPI_MID, true, false>));
+    ALLOW((plane::k_plane_inv<EPI_MID, false, false>));
     ALLOW((plane::k_plane_inv<EPI_LAST, false>));
     ALLOW((plane::k_plane_inv<EPI_MID, false>));
     ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
@@ -579,8 +616,7 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
     a.dst = X;
     a.tw = t.twx;
     a.twl = t.twl;
-    plane::k_plane_fwd<<<dim3(plane::CL, plane::N), plane::THREADS, plane::SMEM_BYTES, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(plane::k_plane_fwd, dim3(plane::CL, plane::N), dim3(plane::THREADS), plane::SMEM_BYTES, s, a);
 }
 
 cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
@@ -589,9 +625,9 @@ cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
         Geometry g{plane::N, plane::N, plane::N, (long long)plane::N * plane::N * plane::N};
         return launch_tensor_zpass(s, X, g, t);
     }
-    plane::k_zpass16<false><<<dim3(plane::N / plane::ZW, plane::N), plane::ZTHREADS, plane::ZSMEM_BYTES, s>>>(
-        X, t.twx, t, plane::N, (long long)plane::N * plane::N);
-    return cudaGetLastError();
+    return launch_pdl(plane::k_zpass16<false>, dim3(plane::N / plane::ZW, plane::N), dim3(plane::ZTHREADS),
+                      plane::ZSMEM_BYTES, s, X, (const float2*)t.twx, t, (int)plane::N,
+                      (long long)plane::N * plane::N);
 }
 
 bool zpass256_supported(const Geometry& g) { return g.nzb == plane::N && g.nxb % plane::ZW == 0; }
@@ -614,16 +650,19 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     a.tw = t.twx;
     a.twl = t.twl;
     a.e = e;
-    const dim3 grid(plane::CL, plane::N);
+    const dim3 grid(plane::CL, plane::N), block(plane::THREADS);
+    const size_t sm = plane::SMEM_BYTES;
+    const bool sum = e.sp.touch;
     if (mode == EPI_FIRST)
-        plane::k_plane_inv<EPI_FIRST, true><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
-    else if (mode == EPI_MID && fwd)
-        plane::k_plane_inv<EPI_MID, true><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
-    else if (mode == EPI_MID)
-        plane::k_plane_inv<EPI_MID, false><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
-    else
-        plane::k_plane_inv<EPI_LAST, false><<<grid, plane::THREADS, plane::SMEM_BYTES, s>>>(a);
-    return cudaGetLastError();
+        return sum ? launch_pdl(plane::k_plane_inv<EPI_FIRST, true>, grid, block, sm, s, a)
+                   : launch_pdl(plane::k_plane_inv<EPI_FIRST, true, false>, grid, block, sm, s, a);
+    if (mode == EPI_MID && fwd)
+        return sum ? launch_pdl(plane::k_plane_inv<EPI_MID, true>, grid, block, sm, s, a)
+                   : launch_pdl(plane::k_plane_inv<EPI_MID, true, false>, grid, block, sm, s, a);
+    if (mode == EPI_MID)
+        return sum ? launch_pdl(plane::k_plane_inv<EPI_MID, false>, grid, block, sm, s, a)
+                   : launch_pdl(plane::k_plane_inv<EPI_MID, false, false>, grid, block, sm, s, a);
+    return launch_pdl(plane::k_plane_inv<EPI_LAST, false>, grid, block, sm, s, a);
 }
 
 // out = v * IFFT3(|k| FFT3(in)) * (sch + scl) with the plane kernels.

@@ -562,7 +562,7 @@ class Modeler:
         return out
 
     def profile_step(self, reps: int = 1):
-        cap = 8
+        cap = 12
         count = ctypes.c_int()
         names = (ctypes.c_char_p * cap)()
         ms = np.zeros(cap, np.float32)
