@@ -25,7 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, HERE)
-from models import layered_noise_model, two_layer_model  # noqa: E402
+from models import layered_noise_model, layered_perturbed_model, two_layer_model  # noqa: E402
 
 CASES = [
     dict(name="small_judge_odd",
@@ -47,12 +47,23 @@ CASES = [
                      nsteps=3, fm=40.0, dt=0.001, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
                      sxbeg=50, sybeg=50, szbeg=0),
          full_fields=False),
+    # the benchmark's config 1 (interior 101^3 + 20-cell sponge, padded 142^3 =
+    # 2 x 71 on every axis; 20 Hz Ricker at (50, 50, 10), dt 2 ms) for a few
+    # steps, with the reference's own sponge and receiver plane (z = 0)
+    dict(name="config1_142",
+         model=dict(kind="layered_perturbed", nx=101, ny=101, nz=101, seed=7),
+         params=dict(nx=101, ny=101, nz=101, bu=20, bd=20, bl=20, br=20, bf=20, bb=20, nt=1000,
+                     nsteps=4, fm=20.0, dt=0.002, amp=100.0, dx=10.0, dy=10.0, dz=10.0,
+                     sxbeg=50, sybeg=50, szbeg=10),
+         full_fields=False),
 ]
 
 
 def make_model(spec):
     if spec["kind"] == "layered_noise":
         return layered_noise_model(spec["nx"], spec["ny"], spec["nz"], spec["seed"])
+    if spec["kind"] == "layered_perturbed":
+        return layered_perturbed_model(spec["nx"], spec["ny"], spec["nz"], spec["seed"])
     return two_layer_model(spec["nx"], spec["ny"], spec["nz"], spec["v_top"], spec["v_bottom"],
                            spec["z_interface"])
 
@@ -126,7 +137,8 @@ def run_case(case, ref_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=os.environ.get("OSE_REF_DIR") or os.path.abspath(
+        os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference")))
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={a.ref_dir}"],

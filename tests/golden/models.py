@@ -23,3 +23,15 @@ def layered_noise_model(nx, ny, nz, seed):
     v = np.broadcast_to(base[None, None, :], (nx, ny, nz)).astype(np.float32)
     v = v * (1.0 + 0.03 * rng.standard_normal((nx, ny, nz))).astype(np.float32)
     return np.ascontiguousarray(v, dtype=np.float32)
+
+
+def layered_perturbed_model(nx, ny, nz, seed):
+    """The config-1 generator of the benchmark workloads (four layers
+    1500/2200/3000/3800 m/s times 1 + a smoothed 5% perturbation)."""
+    import os
+    import sys
+    pkg = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "3d-ose_gb300")
+    if pkg not in sys.path:
+        sys.path.insert(0, pkg)
+    import workloads
+    return workloads.layered_perturbed(nx, ny, nz, seed)

@@ -5,7 +5,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["small_judge_odd", "small_deep_source_odd_nt", "reference_default"]
+CASES = ["small_judge_odd", "small_deep_source_odd_nt", "reference_default", "config1_142"]
 
 
 def load(name):
@@ -17,10 +17,12 @@ def load(name):
 
 
 def model_of(g):
-    from models import layered_noise_model, two_layer_model
+    from models import layered_noise_model, layered_perturbed_model, two_layer_model
     s = g["model_spec"]
     if s["kind"] == "layered_noise":
         return layered_noise_model(s["nx"], s["ny"], s["nz"], s["seed"])
+    if s["kind"] == "layered_perturbed":
+        return layered_perturbed_model(s["nx"], s["ny"], s["nz"], s["seed"])
     return two_layer_model(s["nx"], s["ny"], s["nz"], s["v_top"], s["v_bottom"], s["z_interface"])
 
 
