@@ -235,6 +235,7 @@ cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
         ea.cp = n == 1 ? D.c0 : (n >= 2 ? D.c[n - 2] : 0.f);
         ea.cpl = n == 1 ? D.c0l : (n >= 2 ? D.cl[n - 2] : 0.f);
         ea.sp = ose::sum_plan(n, D.M);
+        ose::set_sum_weights(ea);
         const ose::EpiMode mode = n == 0 ? ose::EPI_FIRST : (n == D.M ? ose::EPI_LAST : ose::EPI_MID);
         e = ose::launch_generic_application(st, D.g, D.px, D.py, D.pz, t, an, D.X, mode, ea, nullptr,
                                             fuse && n > 0, fuse && n < D.M);

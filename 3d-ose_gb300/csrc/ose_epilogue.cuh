@@ -16,21 +16,19 @@ namespace ose {
 enum { EPI_NONE = -1, EPI_SCALE_VEL = 4, EPI_FIRST_FWD = 5, EPI_MID_FWD = 6 };
 
 // The partial-sum update of one cell at a FIRST/MID/LAST application, by the
-// schedule e.sp (SumPlan): s = the stored S (zero unless e.sp.s_read),
-// am = a_{n-1}, an = a_{n+1}, att = the cell's sponge factor.  Branch-free:
-// the powers att^k (k <= kSumMaxPow) are selected, absent terms get factor 0.
+// schedule's weights (EpiArgs::wS, wP, wN): s = the stored S (zero unless
+// it is read), am = a_{n-1}, an = a_{n+1}, att = the cell's sponge factor.
+// Branch-free; a zero weight adds exactly nothing, so each factor is the
+// rounded product of one coefficient and one power of att.
 __device__ __forceinline__ float2 sum_update(const EpiArgs& e, float att, float2 s, float2 am, float2 an)
 {
-    const SumPlan& p = e.sp;
     const float a2 = att * att, a3 = a2 * att;
-    auto pw = [&](int k) { return k == 0 ? 1.f : (k == 1 ? att : (k == 2 ? a2 : a3)); };
-    const float fS = p.s_read ? pw(p.kS) : 0.f;
-    const float gP = p.add_prev ? pw(p.kP) : 0.f;
-    const float gN = p.add_new ? pw(p.kN) : 0.f;
-    const float fP = e.cp * gP, fN = e.c1 * gN;
+    const float fS = fmaf(e.wS[2], a3, fmaf(e.wS[1], a2, e.wS[0] * att));
+    const float fP = fmaf(e.wP[2], a3, fmaf(e.wP[1], a2, e.wP[0] * att));
+    const float fN = e.wN * att;
     float2 r = make_float2(s.x * fS, s.y * fS);
     if (kCompensatedConstants) {
-        const float lP = e.cpl * gP, lN = e.c1l * gN;
+        const float lP = fmaf(e.wPl[2], a3, fmaf(e.wPl[1], a2, e.wPl[0] * att)), lN = e.wNl * att;
         r.x = fmaf(lP, am.x, fmaf(lN, an.x, r.x));
         r.y = fmaf(lP, am.y, fmaf(lN, an.y, r.y));
     }
@@ -170,6 +168,7 @@ __device__ __forceinline__ EpiArgs batch_epi(const BatchShot& S, int n)
     e.cp = n == 1 ? S.c0 : (n >= 2 ? S.c[n - 2] : 0.f);
     e.cpl = n == 1 ? S.c0l : (n >= 2 ? S.cl[n - 2] : 0.f);
     e.sp = sum_plan(n, S.M);
+    set_sum_weights(e);
     e.gather = S.gather;
     e.cur = S.ctr + 1;
     e.gz = S.gz;

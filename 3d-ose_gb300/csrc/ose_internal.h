@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <assert.h>
 #include <stdint.h>
 
 #include <string>
@@ -83,7 +84,9 @@ __host__ __device__ inline SumPlan sum_plan(int n, int M)
     return p;
 }
 
-// The powers a SumPlan uses are 0 .. 3 for every series order M.
+// The powers a SumPlan uses are 0 .. 3 for every series order M up to
+// kMaxTerms (kS, kP in 1 .. 3; kN = 1, or 0 at the first application where
+// att = 1), which the three weights of EpiArgs cover.
 constexpr int kSumMaxPow = 3;
 
 struct EpiArgs {
@@ -99,6 +102,12 @@ struct EpiArgs {
     float c1, c1l;        // coefficient of the new term a_{n+1}: 2 J_{n+1}
     float cp, cpl;        // coefficient of a_{n-1}: J0 (n = 1) or 2 J_{n-1}
     SumPlan sp;           // what this application adds to S
+    // The schedule as weights of att, att^2, att^3 (set_sum_weights): the
+    // stored S is multiplied by sum_k wS[k] att^(k+1), a_{n-1} by
+    // sum_k (wP[k] + wPl[k]) att^(k+1) (one weight nonzero, the coefficient
+    // folded in), a_{n+1} by (wN + wNl) att (its power is 1; the first
+    // application passes att = 1).
+    float wS[3], wP[3], wPl[3], wN, wNl;
     float sch, scl;       // 1 / (R N), the scale of v * IFFT3(|k| FFT3(.))
     // receivers (LAST)
     float* gather;        // [nt][ng]
@@ -147,11 +156,27 @@ inline void split_float(double v, float* hi, float* lo)
 
 // Coefficients and partial-sum schedule of application n of M + 1 (J = the
 // Bessel values J_0 .. J_{M+1} of the step, in double).
+// The weights of EpiArgs from its schedule and coefficients (host and device
+// build the same values: no arithmetic, only placement).
+__host__ __device__ inline void set_sum_weights(EpiArgs& e)
+{
+    const SumPlan& p = e.sp;
+    for (int k = 0; k < 3; ++k) {
+        e.wS[k] = (p.s_read && p.kS == k + 1) ? 1.f : 0.f;
+        e.wP[k] = (p.add_prev && p.kP == k + 1) ? e.cp : 0.f;
+        e.wPl[k] = (p.add_prev && p.kP == k + 1) ? e.cpl : 0.f;
+    }
+    e.wN = p.add_new ? e.c1 : 0.f;
+    e.wNl = p.add_new ? e.c1l : 0.f;
+}
+
 inline void set_application(EpiArgs& e, int n, int M, const double* J)
 {
     split_float(2.0 * J[n + 1], &e.c1, &e.c1l);
     split_float(n == 1 ? J[0] : (n >= 2 ? 2.0 * J[n - 1] : 0.0), &e.cp, &e.cpl);
     e.sp = sum_plan(n, M);
+    assert(e.sp.kS <= kSumMaxPow && e.sp.kP <= kSumMaxPow && e.sp.kN <= 1);
+    set_sum_weights(e);
 }
 
 // HBM bytes per cell of the epilogue of application n (FIRST, MID, LAST):

@@ -51,7 +51,8 @@ constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
-constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N;   // + twiddle table (hi, lo)
+// + twiddle table (hi, lo) + the x sponge factor's powers ax, ax^2, ax^3 (3 N floats)
+constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N + 3 * N / 2;
 constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX;
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -303,7 +304,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 {
     extern __shared__ float4 smem4[];
     float2* smem = reinterpret_cast<float2*>(smem4);
-    float2* tw = smem + (SMEM_COMPLEX - 2 * N);
+    float2* tw = smem + (SMEM_COMPLEX - 2 * N - 3 * N / 2);
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
@@ -329,20 +330,50 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
 // inverse transform on entry and the new term a_{n+1} (FIRST: a_1) on exit.
 // Loads are issued ECH cells at a time ahead of any store; the buffers never
 // overlap at different cells, so the restrict qualifiers are exact.
-// SUM (FIRST, MID): this application updates S (e.sp.touch); LAST always does.
-template <int EPI, bool SUM>
-__device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e, int y, int z, int j)
+// SUM: 0 = S left alone, 1 = S written (its first update of the step),
+// 2 = S read and written (SumPlan: touch, s_read); LAST always has 2.
+// The partial-sum update in this kernel takes the sponge as att = ax[x] *
+// (ay[y] az[z]): the powers of ax come from the shared table axp (axp[(k-1)
+// N + x] = ax[x]^k), those of ay az, times the coefficients, are per row.
+template <int EPI, int SUM>
+__device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e, const float* axp, int y, int z,
+                                              int j)
 {
     float2* __restrict__ prev = e.prev;
     float2* __restrict__ S = e.S;
     float2* __restrict__ wout = e.wout;
     const float* __restrict__ vs = e.vs;
     const size_t rowbase = ((size_t)z * N + y) * N + j;
-    constexpr bool upd = EPI == EPI_LAST || (EPI == EPI_MID && SUM);
+    constexpr bool upd = EPI == EPI_LAST || (EPI == EPI_MID && SUM > 0);
     // cells whose loads are in flight together: fewer where S is read too
-    constexpr int CH = upd ? ECH_SUM : ECH;
-    const bool sread = upd && e.sp.s_read;
+    // and the forward transform of the new term keeps both line slots live
+    constexpr int CH = (SUM == 2 && (EPI == EPI_MID || EPI == EPI_LAST)) ? ECH_SUM : ECH;
+    constexpr bool sread = upd && SUM == 2;
     const float attyz = upd ? __ldg(e.ay + y) * __ldg(e.az + z) : 1.f;
+    // row factors of the schedule (SumPlan): S times ax^kS qS, a_{n-1} times
+    // ax^kP (qP + qPl), a_{n+1} times ax (qN + qNl)
+    const SumPlan& sp = e.sp;
+    const float y2 = attyz * attyz, y3 = y2 * attyz;
+    auto ypow = [&](int k) { return k <= 1 ? attyz : (k == 2 ? y2 : y3); };
+    const float qS = sread ? ypow(sp.kS) : 0.f;
+    const float yP = sp.add_prev ? ypow(sp.kP) : 0.f;
+    const float qP = e.cp * yP, qPl = e.cpl * yP;
+    const float qN = sp.add_new ? e.c1 * attyz : 0.f, qNl = sp.add_new ? e.c1l * attyz : 0.f;
+    const float* axS = axp + (sp.kS > 1 ? sp.kS - 1 : 0) * N;
+    const float* axP = axp + (sp.kP > 1 ? sp.kP - 1 : 0) * N;
+    auto update = [&](float2 s, float2 am, float2 an, int x) {
+        const float ax = axp[x], fS = axS[x] * qS, aP = axP[x];
+        const float fP = aP * qP, fN = ax * qN;
+        float2 r = make_float2(s.x * fS, s.y * fS);
+        if (kCompensatedConstants) {
+            const float lP = aP * qPl, lN = ax * qNl;
+            r.x = fmaf(lP, am.x, fmaf(lN, an.x, r.x));
+            r.y = fmaf(lP, am.y, fmaf(lN, an.y, r.y));
+        }
+        r.x = fmaf(fP, am.x, fmaf(fN, an.x, r.x));
+        r.y = fmaf(fP, am.y, fmaf(fN, an.y, r.y));
+        return r;
+    };
 #pragma unroll
     for (int h = 0; h < 16 / CH; ++h) {
         float vv[CH];
@@ -376,10 +407,10 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
                 const float2 an = make_float2(fmaf(2.f, Lx.y, am[q].x), fmaf(-2.f, Lx.x, am[q].y));
                 if (EPI == EPI_MID) {
                     prev[i] = an;
-                    if (upd) S[i] = sum_update(e, __ldg(e.ax + x) * attyz, sm[q], am[q], an);
+                    if (upd) S[i] = update(sm[q], am[q], an, x);
                     v[n1] = an;
                 } else {
-                    const float2 s = sum_update(e, __ldg(e.ax + x) * attyz, sm[q], am[q], an);
+                    const float2 s = update(sm[q], am[q], an, x);
                     wout[i] = s;
                     if (z == e.gz) {
                         const int ix = x - e.bl, iy = y - e.bf;
@@ -396,15 +427,24 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
 
 // Inverse y and x FFTs of plane z, the pointwise update, and (FWD) the
 // forward x and y FFTs of the new term.
-template <int EPI, bool FWD, bool SUM = true>
+template <int EPI, bool FWD, int SUM = 2>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane_inv(Args a)
 {
     extern __shared__ float4 smem4[];
     float2* smem = reinterpret_cast<float2*>(smem4);
-    float2* tw = smem + (SMEM_COMPLEX - 2 * N);
+    float2* tw = smem + (SMEM_COMPLEX - 2 * N - 3 * N / 2);
+    float* axp = reinterpret_cast<float*>(tw + 2 * N);
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
+    if (EPI == EPI_MID || EPI == EPI_LAST) {
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            const float ax = __ldg(a.e.ax + t);
+            axp[t] = ax;
+            axp[N + t] = ax * ax;
+            axp[2 * N + t] = ax * ax * ax;
+        }
+    }
     // The epilogue's operands of this CTA's 32 rows are contiguous: start
     // pulling them into L2 now, so the epilogue's loads hit L2 (v is constant;
     // a_{n-1} and S only once the kernels that wrote them have completed).
@@ -415,7 +455,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     griddep_wait();
     if (threadIdx.x == 0 && EPI != EPI_SCALE && EPI != EPI_FIRST) {
         prefetch_l2(a.e.prev + row0, SL * N * sizeof(float2));
-        if (SUM && a.e.sp.s_read) prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
+        if (SUM == 2) prefetch_l2(a.e.S + row0, SL * N * sizeof(float2));
     }
     float2 v0[16], v1[16];
     // spectrum columns 32r..: thread (c, j) takes ky = j + 16 k2
@@ -455,14 +495,17 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     cluster.sync();
     fft256<true, true>(T, tw, v0, v1);
     // pointwise update on (x = 16 n1 + j, y, z)
-    epilogue_slot<EPI, SUM>(v0, a.e, SL * r + row_slot(0).row, z, row_slot(0).j);
-    if (NS > 1) epilogue_slot<EPI, SUM>(v1, a.e, SL * r + row_slot(1).row, z, row_slot(1).j);
+    epilogue_slot<EPI, SUM>(v0, a.e, axp, SL * r + row_slot(0).row, z, row_slot(0).j);
+    if (NS > 1) epilogue_slot<EPI, SUM>(v1, a.e, axp, SL * r + row_slot(1).row, z, row_slot(1).j);
     if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
 }
 
 // z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
 // One line slot per thread (column c = t % 16, line thread j = t / 16) keeps
 // registers near 64 so four CTAs share an SM.
+#ifndef OSE_ZPASS_MINB
+#define OSE_ZPASS_MINB 4
+#endif
 constexpr int ZW = 16;
 constexpr int ZTHREADS = 256;
 constexpr size_t ZSMEM_BYTES = sizeof(float2) * (16 * 16 * ZW + 2 * N);
@@ -483,7 +526,7 @@ __device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, f
 // strides cost registers: the GRID form spills a little at this bound, which
 // measured faster than three CTAs per SM without most of the spills).
 template <bool GRID>
-__global__ void __launch_bounds__(ZTHREADS, 4) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
+__global__ void __launch_bounds__(ZTHREADS, OSE_ZPASS_MINB) k_zpass16(float2* __restrict__ X, const float2* __restrict__ gtw,
                                                          Tables t, int nxb_arg, long long plane_arg)
 {
     extern __shared__ float4 smem4[];
@@ -595,11 +638,13 @@ cudaError_t configure_plane_kernels()
         cudaSuccess)                                                                          \
         return e
     ALLOW(plane::k_plane_fwd);
-    ALLOW((plane::k_plane_inv<EPI_FIRST, true>));
-    ALLOW((plane::k_plane_inv<EPI_FIRST, true, false>));
-    ALLOW((plane::k_plane_inv<EPI_MID, true>));
-    ALLOW((plane::k_plane_inv<EPI_MID, true, false>));
-    ALLOW((plane::k_plane_inv<EPI_MID, false, false>));
+    ALLOW((plane::k_plane_inv<EPI_FIRST, true, 0>));
+    ALLOW((plane::k_plane_inv<EPI_FIRST, true, 1>));
+    ALLOW((plane::k_plane_inv<EPI_MID, true, 0>));
+    ALLOW((plane::k_plane_inv<EPI_MID, true, 1>));
+    ALLOW((plane::k_plane_inv<EPI_MID, true, 2>));
+    ALLOW((plane::k_plane_inv<EPI_MID, false, 0>));
+    ALLOW((plane::k_plane_inv<EPI_MID, false, 1>));
     ALLOW((plane::k_plane_inv<EPI_LAST, false>));
     ALLOW((plane::k_plane_inv<EPI_MID, false>));
     ALLOW((plane::k_plane_inv<EPI_SCALE, false>));
@@ -652,17 +697,21 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     a.e = e;
     const dim3 grid(plane::CL, plane::N), block(plane::THREADS);
     const size_t sm = plane::SMEM_BYTES;
-    const bool sum = e.sp.touch;
-    if (mode == EPI_FIRST)
-        return sum ? launch_pdl(plane::k_plane_inv<EPI_FIRST, true>, grid, block, sm, s, a)
-                   : launch_pdl(plane::k_plane_inv<EPI_FIRST, true, false>, grid, block, sm, s, a);
+    const int sum = e.sp.touch ? (e.sp.s_read ? 2 : 1) : 0;
+    if (mode == EPI_FIRST)   // the first application never reads S
+        return sum ? launch_pdl(plane::k_plane_inv<EPI_FIRST, true, 1>, grid, block, sm, s, a)
+                   : launch_pdl(plane::k_plane_inv<EPI_FIRST, true, 0>, grid, block, sm, s, a);
     if (mode == EPI_MID && fwd)
-        return sum ? launch_pdl(plane::k_plane_inv<EPI_MID, true>, grid, block, sm, s, a)
-                   : launch_pdl(plane::k_plane_inv<EPI_MID, true, false>, grid, block, sm, s, a);
+        return sum == 2 ? launch_pdl(plane::k_plane_inv<EPI_MID, true, 2>, grid, block, sm, s, a)
+               : sum == 1 ? launch_pdl(plane::k_plane_inv<EPI_MID, true, 1>, grid, block, sm, s, a)
+                          : launch_pdl(plane::k_plane_inv<EPI_MID, true, 0>, grid, block, sm, s, a);
     if (mode == EPI_MID)
-        return sum ? launch_pdl(plane::k_plane_inv<EPI_MID, false>, grid, block, sm, s, a)
-                   : launch_pdl(plane::k_plane_inv<EPI_MID, false, false>, grid, block, sm, s, a);
-    return launch_pdl(plane::k_plane_inv<EPI_LAST, false>, grid, block, sm, s, a);
+        return sum == 2 ? launch_pdl(plane::k_plane_inv<EPI_MID, false, 2>, grid, block, sm, s, a)
+               : sum == 1 ? launch_pdl(plane::k_plane_inv<EPI_MID, false, 1>, grid, block, sm, s, a)
+                          : launch_pdl(plane::k_plane_inv<EPI_MID, false, 0>, grid, block, sm, s, a);
+    // LAST always reads S: an earlier application of every step stores it
+    if (sum != 2) return cudaErrorInvalidValue;
+    return launch_pdl(plane::k_plane_inv<EPI_LAST, false, 2>, grid, block, sm, s, a);
 }
 
 // out = v * IFFT3(|k| FFT3(in)) * (sch + scl) with the plane kernels.

@@ -175,6 +175,31 @@ def oracle_rate(kw, vel, nsteps: int, warm: int = 0):
     return cells * nsteps / max(t, 1e-9) / 1e9, O.threads(), t
 
 
+def accuracy_vs_fp64(m, kw, vel, shot: int, nsteps: int):
+    """Checker leg (outside every timed region): rel-L2 of the modeler's
+    receiver gather over its first nsteps steps and of its P and Q after them,
+    against the FP64 restatement of the same loop (oracle/oracle_torch.py,
+    torch complex128 on the same GPU) run from the same start for the same
+    steps."""
+    import ose3d
+    from oracle_torch import TorchOracle
+    t0 = time.perf_counter()
+    g = m.gather()[:, :nsteps].T.astype(np.float64)
+    P = m.wavefield(ose3d.FIELD_P)
+    Q = m.wavefield(ose3d.FIELD_Q)
+    o = TorchOracle(kw, vel, "cuda", shot=shot)
+    g64 = o.run(nsteps)
+    P64, Q64 = o.P(), o.Q()
+    del o
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+    return {"steps": nsteps, "gather_rel_l2": rel(g, g64), "P_rel_l2": rel(P, P64), "Q_rel_l2": rel(Q, Q64),
+            "bar": 1e-4, "vs": "FP64 restatement of the same loop (torch complex128 on the same GPU)",
+            "check_s": round(time.perf_counter() - t0, 1)}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
@@ -411,7 +436,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-accuracy", action="store_true", help="learned workload: timing only")
+    ap.add_argument("--no-accuracy", action="store_true", help="timing only (no FP64 check)")
+    ap.add_argument("--accuracy-steps", type=int, default=300,
+                    help="steps of the shot compared with the FP64 restatement (the timed steps included)")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end job (0: the workload's nt)")
     ap.add_argument("--workload", default=WORKLOAD,
                     choices=[WORKLOAD, "ose320x288x256", "ose384x384x256", "ose142", "ose142cerjan", "batched64",
                              "precision", "learned"])
@@ -460,6 +488,15 @@ def main():
     ms = dist.max(ms)
     value = replica_rate(world, cells, args.steps, ms)
 
+    # accuracy of this shot against FP64 (rank 0): the timed steps plus
+    # untimed ones up to --accuracy-steps, then gather, P and Q compared
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        acc_steps = min(max(args.accuracy_steps, warm + args.steps), kw["nt"] - 3)
+        if acc_steps > warm + args.steps:
+            m.run(acc_steps - (warm + args.steps))
+        accuracy = accuracy_vs_fp64(m, kw, vel, rank, acc_steps)
+
     # per-kernel launch durations (events bracketing each launch, one step)
     rows, launches_per_step = m.profile_step(reps=2)
     per_step = {r["name"]: r["launches_per_step"] for r in rows}
@@ -478,24 +515,28 @@ def main():
                 (ms * 1e-3 / args.steps) / 1e9}
     m.close()
 
-    # end to end through the C ABI from host buffers: create (model upload),
-    # reset (wavelets), K steps each copying its receiver row to the host,
-    # final P and Q back to the host
+    # end to end through the C ABI from host buffers, the whole job of the
+    # workload (its nt steps, as the reference's main runs it): create (model
+    # upload), reset (wavelets), every step copying its receiver row to the
+    # host, final P and Q back to the host
+    e2e_steps = kw["nt"] if args.e2e_steps <= 0 else min(args.e2e_steps, kw["nt"])
     device_sync()
     t0 = time.perf_counter()
     m2 = ose3d.Modeler(params, vel)
     m2.reset_shot(rank)
-    rows_out = m2.run_record(args.steps)
+    rows_out = m2.run_record(e2e_steps)
     q = m2.wavefield(ose3d.FIELD_Q)
     p_ = m2.wavefield(ose3d.FIELD_P)
     t_e2e = time.perf_counter() - t0
     m2.close()
     t_e2e = dist.max(t_e2e)
-    h2d = (vel.nbytes + 2 * 4 * kw["nt"]) / args.steps
-    d2h = (rows_out.nbytes + q.nbytes + p_.nbytes) / args.steps
-    e2e = {"value": replica_rate(world, cells, args.steps, t_e2e * 1e3), "unit": UNIT,
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "timing": "host wall clock around create + reset_shot + run_record + wavefield reads"}
+    h2d = (vel.nbytes + 2 * 4 * kw["nt"]) / e2e_steps
+    d2h = (rows_out.nbytes + q.nbytes + p_.nbytes) / e2e_steps
+    e2e = {"value": replica_rate(world, cells, e2e_steps, t_e2e * 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+           "seconds": round(t_e2e, 3),
+           "timing": "host wall clock around create + reset_shot + run_record (one receiver row to the host per "
+                     "step) + final P and Q reads, over the workload's whole job"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -512,7 +553,7 @@ def main():
                        "M": d.M, "kernel_path": "generic" if d.path == 0 else "plane",
                        "l2": f"inputs larger than L2 (each field {cells * 8 / 1e6:.0f} MB)",
                        "parallelism": f"replicas x{world} (one independent shot per GPU)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
             "gpu_launches": launches_per_step * args.steps, "clocks": clocks}
     print(json.dumps(line), flush=True)
     return 0
