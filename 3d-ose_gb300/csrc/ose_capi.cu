@@ -250,7 +250,9 @@ cudaError_t enqueue_step_plane(ose_handle* h, ose::KernelTiming* tm, bool source
         ose::set_application(ea, n, M, h->J.data());
         const bool fwd = n < M;
         const double bytes = ose::epilogue_bytes(mode, ea.sp, fwd) * N;
-        const int cls = mode == ose::EPI_FIRST ? 2 : (mode == ose::EPI_LAST ? 4 : (ea.sp.touch ? 3 : 8));
+        // classes: 3 MID reading and writing S, 9 MID starting S, 8 MID leaving S alone
+        const int cls = mode == ose::EPI_FIRST ? 2
+                        : (mode == ose::EPI_LAST ? 4 : (ea.sp.touch ? (ea.sp.s_read ? 3 : 9) : 8));
         e = timed(tm, s, cls, bytes, [&] { return ose::launch_plane_inv(s, mode, fwd, h->X, h->X, h->tables, ea); });
         if (e != cudaSuccess) return e;
     }
@@ -1189,7 +1191,7 @@ ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count, const 
                                      "fft_x_inv_epilogue_nosum", "unused"};
     static const char* kPlane[] = {"plane_fwd", "zpass", "plane_inv_first", "plane_inv_mid",
                                    "plane_inv_last", "inject", "corrector_scale", "corrector",
-                                   "plane_inv_mid_nosum", "unused"};
+                                   "plane_inv_mid_nosum", "plane_inv_mid_sumstart"};
     const char** kNames = h->d.path == OSE_PATH_PLANE ? kPlane : kGeneric;
     for (int c = 0; c < ose::KernelTiming::kClasses; ++c) { t.ms[c] = 0.f; t.count[c] = 0; t.bytes[c] = 0.0; }
     for (int r = 0; r < reps; ++r) {
