@@ -233,6 +233,7 @@ def main():
     t.add_argument("--n", type=int, default=48)
     t.add_argument("--steps", type=int, default=150)
     t.add_argument("--every", type=int, default=5)
+    t.add_argument("--t0", type=int, default=20, help="first step sampled")
     t.add_argument("--epochs", type=int, default=4)
     t.add_argument("--batch", type=int, default=16)
     t.add_argument("--lr", type=float, default=1e-3)
@@ -248,7 +249,7 @@ def main():
     a = ap.parse_args()
     if a.cmd == "train":
         t0 = time.time()
-        data = generate(a.runs, a.seed, n=a.n, steps=a.steps, every=a.every)
+        data = generate(a.runs, a.seed, n=a.n, steps=a.steps, t0=a.t0, every=a.every)
         t_gen = time.time() - t0
         params, hist = train(data, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed,
                              init=np.load(a.init) if a.init else None)

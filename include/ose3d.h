@@ -291,8 +291,9 @@ ose_status ose_apply_operator(ose_handle* h, const float* in, float* out);
  * measured with CUDA events bracketing each launch on the handle's stream
  * (not graph replay).  Advances the shot by `reps` steps.  names, ms, bytes
  * and launches are arrays of capacity cap; *count receives the number of
- * classes.  bytes = algorithmic HBM bytes of one launch; launches = launches
- * of the class per step. */
+ * classes that launched in those steps (the source injection always listed).
+ * bytes = algorithmic HBM bytes of one launch; launches = launches of the
+ * class per step. */
 ose_status ose_profile_step(ose_handle* h, int reps, int cap, int* count,
                             const char** names, float* ms, double* bytes,
                             int* launches);

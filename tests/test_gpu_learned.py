@@ -6,7 +6,9 @@ same run without it, both measured against the 64-cell-sponge run.
 Measured when the weights were made (4 held-out cases, 300 steps): interior
 error energy 0.24-0.42 without, 0.022-0.050 with the corrector (gain 8-11x);
 gather rel-L2 0.63-1.48 without, 0.31-0.45 with.  On the two cases of this
-test (200 steps) the gains were 6.0x and 6.8x; the test asks for 4x."""
+test (200 steps) the gains were 6.0x and 6.8x; the test asks for 4x.  At twice
+the training size (interior 96^3, 112^3 thin grid against 224^3 wide, 300
+steps, two held-out cases) the gains were 5.1x and 7.1x; asked: 4x."""
 import os
 
 import numpy as np
@@ -24,13 +26,14 @@ def built():
     ose3d.load_library()
 
 
-def test_trained_corrector_reduces_boundary_error():
+@pytest.mark.parametrize("n,steps,seed", [(48, 200, 4242), (96, 300, 777)])
+def test_trained_corrector_reduces_boundary_error(n, steps, seed):
     pytest.importorskip("torch")
     import learn_boundary as LB
     assert os.path.exists(LB.WEIGHTS)
     params = np.load(LB.WEIGHTS)
     assert params.size == ose3d.corrector_param_count()
-    res = LB.evaluate(params, seed=4242, cases=2, n=48, steps=200)
+    res = LB.evaluate(params, seed=seed, cases=2, n=n, steps=steps)
     for r in res:
         print(f"fm {r['fm']:.1f} Hz: error energy {r['plain']['interior_error_energy']:.3e} -> "
               f"{r['learned']['interior_error_energy']:.3e} (gain {r['gain']:.1f}x), gather "

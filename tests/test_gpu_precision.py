@@ -17,8 +17,13 @@ from golden_util import rel_l2
 pytestmark = pytest.mark.gpu
 
 TOL = {"fp32": 1e-6, "tf32": 1e-3, "tf32x3": 2e-6, "bf16x3": 2e-5}
-# 40 steps on a rough random model (gather and final Q)
-TOL_STEPS = {"fp32": 5e-5, "tf32x3": 5e-5, "bf16x3": 3e-4}
+# 40 steps on a rough random model (gather and final Q).  FP32 and TF32X3
+# meet the 1e-4 parity bar of the FP32 path with room to spare; BF16X3 (about
+# 16 significant bits per product) does not meet it and is held to the bound
+# of its own arithmetic class; single-pass TF32 is far outside both.
+TOL_STEPS = {"fp32": 5e-5, "tf32x3": 5e-5}
+PARITY_BAR = 1e-4
+TOL_STEPS_BF16X3 = 3e-4
 
 # padded 32 x 24 x 256
 KW = dict(nx=12, ny=8, nz=216, bu=20, bd=20, bl=10, br=10, bf=8, bb=8, nt=40, fm=30.0, dt=0.001,
@@ -55,9 +60,7 @@ def test_operator_matches_oracle(vel, mode):
     assert err < TOL[mode]
 
 
-@pytest.mark.parametrize("mode", ["fp32", "tf32x3", "bf16x3"])
-def test_steps_match_oracle(vel, mode):
-    """40 steps (gather and final Q) against the FP64 C oracle."""
+def _steps_error(vel, mode):
     p = O.make_params(**KW)
     with ose3d.Modeler(ose3d.default_params(**KW), vel) as m:
         m.precision = mode
@@ -67,7 +70,23 @@ def test_steps_match_oracle(vel, mode):
     G, P, Q = O.run(p, vel, KW["nt"])
     eg, eq = rel_l2(g, G), rel_l2(q, Q)
     print(f"40 steps {mode}: gather {eg:.3e} Q {eq:.3e}")
+    return eg, eq
+
+
+@pytest.mark.parametrize("mode", ["fp32", "tf32x3"])
+def test_steps_meet_parity_bar(vel, mode):
+    """40 steps (gather and final Q) against the FP64 C oracle, inside the
+    1e-4 bar."""
+    eg, eq = _steps_error(vel, mode)
     assert eg < TOL_STEPS[mode] and eq < TOL_STEPS[mode]
+    assert max(eg, eq) < PARITY_BAR
+
+
+def test_bf16x3_steps_within_its_class(vel):
+    """BF16X3 after 40 steps: within the bound of its arithmetic class, which
+    is above the 1e-4 parity bar (the variant does not meet it)."""
+    eg, eq = _steps_error(vel, "bf16x3")
+    assert eg < TOL_STEPS_BF16X3 and eq < TOL_STEPS_BF16X3
 
 
 def test_switching_back_to_fp32_is_bitwise(vel):
