@@ -45,9 +45,13 @@ constexpr int THREADS = 512 / NS;
 constexpr int WARPS = THREADS / 32;
 constexpr int ECH = NS == 1 ? 4 : 8;   // epilogue cells loaded ahead of their stores
 #ifndef OSE_PLANE_ECH_SUM
-#define OSE_PLANE_ECH_SUM 4
+#define OSE_PLANE_ECH_SUM 8
 #endif
 constexpr int ECH_SUM = OSE_PLANE_ECH_SUM;   // the same where S is read and written too
+#ifndef OSE_PLANE_ECH_LAST
+#define OSE_PLANE_ECH_LAST 8
+#endif
+constexpr int ECH_LAST = OSE_PLANE_ECH_LAST;  // the last application (S read, the state written)
 constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
@@ -337,9 +341,9 @@ __device__ __forceinline__ void epilogue_slot(float2 (&v)[16], const EpiArgs& e,
     const float* __restrict__ vs = e.vs;
     const size_t rowbase = ((size_t)z * N + y) * N + j;
     constexpr bool upd = EPI == EPI_LAST || (EPI == EPI_MID && SUM > 0);
-    // cells whose loads are in flight together: fewer where S is read too
-    // and the forward transform of the new term keeps both line slots live
-    constexpr int CH = (SUM == 2 && (EPI == EPI_MID || EPI == EPI_LAST)) ? ECH_SUM : ECH;
+    // cells whose loads are in flight together (8 everywhere: measured
+    // fastest, with a few spilled registers in the last application)
+    constexpr int CH = SUM == 2 ? (EPI == EPI_MID ? ECH_SUM : (EPI == EPI_LAST ? ECH_LAST : ECH)) : ECH;
     constexpr bool sread = upd && SUM == 2;
     const float attyz = upd ? __ldg(e.ay + y) * __ldg(e.az + z) : 1.f;
     // row factors of the schedule (SumPlan): S times ax^kS qS, a_{n-1} times
