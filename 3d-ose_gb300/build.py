@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            "--expt-relaxed-constexpr", "-I" + INCLUDE]
 SOURCES = ["ose_kernels.cu", "ose_plane.cu", "ose_capi.cu", "ose_host.cpp", "ose_noalloc.cu", "ose_io.cpp",
-           "ose_batch.cu", "ose_tensor.cu", "ose_learn.cu", "ose_learn_tc.cu", "ose_cols.cu"]
+           "ose_batch.cu", "ose_tensor.cu", "ose_learn.cu", "ose_learn_tc.cu", "ose_cols.cu", "ose_bluestein.cu"]
 
 
 def nvcc() -> str:

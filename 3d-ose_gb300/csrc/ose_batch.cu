@@ -226,7 +226,7 @@ cudaError_t enqueue_shot_step(ose_batch* b, int s, cudaStream_t st)
     ea.nx = D.nx;
     ea.ny = D.ny;
     ea.nt = D.nt;
-    const bool fuse = ose::generic_fuses_x(D.px);   // as the single-shot step
+    const bool fuse = ose::generic_fuses_x(D.px, t);   // as the single-shot step
     for (int n = 0; n <= D.M; ++n) {
         const float2* an = n == 0 ? D.W : ((n & 1) ? D.A : D.W);
         ea.prev = n == 0 ? D.A : ((n & 1) ? D.W : D.A);

@@ -40,6 +40,7 @@ struct ose_handle {
     float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
     float *kx2l = nullptr, *ky2l = nullptr, *kz2l = nullptr;   // low parts
     float2* twxl = nullptr;                                     // low parts of W_nxb
+    float2* bluetab[3] = {};                                    // Bluestein tables per axis
     float sch = 0.f, scl = 0.f;                                 // 1 / (R N) as hi + lo
     float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
     float *ricker = nullptr, *hil = nullptr;
@@ -130,6 +131,8 @@ void free_all(ose_handle* h)
                     h->twx, h->twy, h->twz, h->ricker, h->hil, h->gather, h->ctr,
                     h->kx2l, h->ky2l, h->kz2l, h->twxl, h->tcb, h->tcerr, h->rec_idx};
     for (void* b : bufs)
+        if (b) cudaFree(b);
+    for (float2* b : h->bluetab)
         if (b) cudaFree(b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -290,7 +293,7 @@ cudaError_t enqueue_step(ose_handle* h, ose::KernelTiming* tm, bool source = tru
     const double N = (double)h->g.ncell;
     // with the register row kernels, the row pass of application n also
     // writes the x transform of a_{n+1}, so application n + 1 skips its x pass
-    const bool fuse = ose::generic_fuses_x(h->px);
+    const bool fuse = ose::generic_fuses_x(h->px, h->tables);
     for (int n = 0; n <= M; ++n) {
         // n = 0: a_1 = -i L a_0 from a_0 = W
         const float2* an = n == 0 ? h->W : ((n & 1) ? h->A : h->W);
@@ -528,6 +531,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(ose::configure_kernels());
     CKC(ose::configure_plane_kernels());
     CKC(ose::configure_tensor_kernels());
+    CKC(ose::configure_bluestein_kernels());
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
@@ -576,6 +580,27 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     CKC(upload(h, h->twx, twx));
     CKC(upload(h, h->twy, twy));
     CKC(upload(h, h->twz, twz));
+    // axes without register kernels of their own: Bluestein tables (chirp,
+    // spectrum, W_L) in one buffer per axis (none for a 256-long axis)
+    std::vector<float2> blue_all[3];
+    {
+        const int ns[3] = {d.nxb, d.nyb, d.nzb};
+        for (int a = 0; a < 3; ++a) {
+            const int L = ose::bluestein_length(ns[a]);
+            h->tables.bl[a] = L;
+            if (!L) continue;
+            std::vector<float2> ch, sp, tw;
+            ose::bluestein_tables(ns[a], L, ch, sp, tw);
+            blue_all[a] = ch;
+            blue_all[a].insert(blue_all[a].end(), sp.begin(), sp.end());
+            blue_all[a].insert(blue_all[a].end(), tw.begin(), tw.end());
+            CKC(dalloc(h, &h->bluetab[a], blue_all[a].size()));
+            CKC(upload(h, h->bluetab[a], blue_all[a]));
+            h->tables.bch[a] = h->bluetab[a];
+            h->tables.bsp[a] = h->bluetab[a] + ns[a];
+            h->tables.btw[a] = h->bluetab[a] + ns[a] + L;
+        }
+    }
     CKC(cudaMemsetAsync(h->W, 0, sizeof(float2) * N, h->stream));
     CKC(cudaMemsetAsync(h->ctr, 0, sizeof(int) * 4, h->stream));
     CKC(cudaStreamSynchronize(h->stream));
@@ -591,6 +616,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     h->tables.kx2l = h->kx2l;
     h->tables.ky2l = h->ky2l;
     h->tables.kz2l = h->kz2l;
+
     d.path = ose::plane_path_supported(d.nxb, d.nyb, d.nzb) ? OSE_PATH_PLANE : OSE_PATH_GENERIC;
     if (const char* env = getenv("OSE3D_PATH"))
         if (!strcmp(env, "generic")) d.path = OSE_PATH_GENERIC;

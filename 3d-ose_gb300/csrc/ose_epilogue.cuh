@@ -85,10 +85,11 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
 // i = i0 + k * xs: every load of a chunk of 8 cells is issued before the
 // first store, so the loads overlap (the per-cell arithmetic is epilogue's).
 // KEEP (FIRST, MID): v also receives the new term a_{n+1}, for the next
-// application's forward transform in the same kernel.
+// application's forward transform in the same kernel.  Only the first
+// `valid` cells exist (a row shorter than CNT * xs); the others are left alone.
 template <int EPI, int CNT, bool KEEP = false>
 __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int x0, int xs, int y, int z,
-                                             const EpiArgs& e)
+                                             const EpiArgs& e, int valid = CNT)
 {
     constexpr int CH = 8;
     static_assert(CNT % CH == 0, "whole chunks");
@@ -100,6 +101,7 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
         for (int q = 0; q < CH; ++q) {
             const int k = CH * h + q;
             const long long i = i0 + (long long)k * xs;
+            if (k >= valid) continue;
             vv[q] = __ldg(e.vs + i);
             if (EPI == EPI_MID || EPI == EPI_LAST) {
                 am[q] = e.prev[i];
@@ -117,6 +119,7 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
             const int k = CH * h + q;
             const long long i = i0 + (long long)k * xs;
             const int x = x0 + k * xs;
+            if (k >= valid) continue;
             const float2 X = v[k];
             float2 Lx = make_float2(X.x * vv[q], X.y * vv[q]);
             if (kCompensatedConstants || EPI == EPI_SCALE_VEL)

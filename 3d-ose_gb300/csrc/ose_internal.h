@@ -131,6 +131,13 @@ struct Tables {
     int tcvar;
     const void* tcb;
     int* tcerr;
+    // Bluestein transforms (ose_bluestein.cu), per axis x, y, z: length L of
+    // the register transforms (0 = the axis has its own kernels), chirp (n),
+    // B = FFT_L(b) / L and W_L^t (L each)
+    int bl[3];
+    const float2* bch[3];
+    const float2* bsp[3];
+    const float2* btw[3];
 };
 
 // Compensated constants: when true, the Bessel coefficients, 1/(R N) and |k|
@@ -198,7 +205,7 @@ struct KernelTiming;
 // register row kernels (generic_fuses_x): x_ready = X already holds the x
 // transform of an (pass 1 skipped); fwd_next (FIRST, MID) = the row pass also
 // writes the x transform of the new term into X for the next application.
-bool generic_fuses_x(const AxisPlan& px);
+bool generic_fuses_x(const AxisPlan& px, const Tables& t);
 cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                        const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                        const float2* an, float2* X, EpiMode mode,
@@ -244,6 +251,16 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
 cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2* X, float2* out,
                                         const float* vs, float sch, float scl, const Tables& t);
 int plane_max_active_clusters();
+
+// Axis transforms by Bluestein's chirp-z identity (ose_bluestein.cu).
+int bluestein_length(int n);
+void bluestein_tables(int n, int L, std::vector<float2>& chirp, std::vector<float2>& spec,
+                      std::vector<float2>& twl);
+cudaError_t configure_bluestein_kernels();
+cudaError_t launch_col_bluestein(cudaStream_t s, int mode, int n, float2* X, int nxb, int nother, long long stride,
+                                 long long ostride, int axis, const Tables& t);
+cudaError_t launch_row_bluestein(cudaStream_t s, int epi, int n, const float2* src, float2* dst, int nyb,
+                                 long long nrows, const Tables& t, const EpiArgs& e);
 
 // Precision form: tensor-core z pass (ose_tensor.cu).
 bool tensor_zpass_supported(int nxb, int nyb, int nzb);

@@ -351,7 +351,10 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     const long long nrows = (long long)g.nyb * g.nzb;
     if (!x_ready) {
         Timer T(tm, s, T_XF);
-        if (use_col_kernels() && col_supported(px.n)) {
+        if (t.bl[0]) {
+            cudaError_t e = launch_row_bluestein(s, EPI_NONE, px.n, an, X, g.nyb, nrows, t, none);
+            if (e != cudaSuccess) return e;
+        } else if (use_col_kernels() && col_supported(px.n)) {
             cudaError_t e = launch_row(s, EPI_NONE, px.n, an, X, g.nyb, nrows, t.twx, none);
             if (e != cudaSuccess) return e;
         } else {
@@ -366,7 +369,10 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     const bool zcols = use_col_kernels() && col_supported(pz.n);
     {
         Timer T(tm, s, T_YF);
-        if (ycols) {
+        if (t.bl[1]) {
+            cudaError_t e = launch_col_bluestein(s, 0, py.n, X, g.nxb, g.nzb, g.nxb, plane, 1, t);
+            if (e != cudaSuccess) return e;
+        } else if (ycols) {
             cudaError_t e = launch_col(s, 0, py.n, X, g.nxb, g.nzb, g.nxb, plane, t.twy, t);
             if (e != cudaSuccess) return e;
         } else {
@@ -384,6 +390,9 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
         } else if (use_col_kernels() && zpass256_supported(g)) {
             cudaError_t e = launch_zpass256(s, X, g, t);
             if (e != cudaSuccess) return e;
+        } else if (t.bl[2]) {
+            cudaError_t e = launch_col_bluestein(s, 2, pz.n, X, g.nxb, g.nyb, plane, g.nxb, 2, t);
+            if (e != cudaSuccess) return e;
         } else if (zcols) {
             cudaError_t e = launch_col(s, 2, pz.n, X, g.nxb, g.nyb, plane, g.nxb, t.twz, t);
             if (e != cudaSuccess) return e;
@@ -396,7 +405,10 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     }
     {
         Timer T(tm, s, T_YI);
-        if (ycols) {
+        if (t.bl[1]) {
+            cudaError_t e = launch_col_bluestein(s, 1, py.n, X, g.nxb, g.nzb, g.nxb, plane, 1, t);
+            if (e != cudaSuccess) return e;
+        } else if (ycols) {
             cudaError_t e = launch_col(s, 1, py.n, X, g.nxb, g.nzb, g.nxb, plane, t.twy, t);
             if (e != cudaSuccess) return e;
         } else {
@@ -409,14 +421,17 @@ static cudaError_t passes_1_to_4(cudaStream_t s, const Geometry& g, const AxisPl
     return cudaGetLastError();
 }
 
-bool generic_fuses_x(const AxisPlan& px) { return use_col_kernels() && col_supported(px.n); }
+bool generic_fuses_x(const AxisPlan& px, const Tables& t)
+{
+    return t.bl[0] != 0 || (use_col_kernels() && col_supported(px.n));
+}
 
 cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const AxisPlan& px,
                                        const AxisPlan& py, const AxisPlan& pz, const Tables& t,
                                        const float2* an, float2* X, EpiMode mode, const EpiArgs& e,
                                        KernelTiming* tm, bool x_ready, bool fwd_next)
 {
-    const bool fuse = generic_fuses_x(px);
+    const bool fuse = generic_fuses_x(px, t);
     cudaError_t err = passes_1_to_4(s, g, px, py, pz, t, an, X, tm, fuse && x_ready);
     if (err != cudaSuccess) return err;
     const long long nrows = (long long)g.nyb * g.nzb;
@@ -427,7 +442,8 @@ cudaError_t launch_generic_application(cudaStream_t s, const Geometry& g, const 
         int epi = (int)mode;
         if (fwd_next && mode == EPI_FIRST) epi = EPI_FIRST_FWD;
         if (fwd_next && mode == EPI_MID) epi = EPI_MID_FWD;
-        err = launch_row(s, epi, px.n, X, X, g.nyb, nrows, t.twx, e);
+        err = t.bl[0] ? launch_row_bluestein(s, epi, px.n, X, X, g.nyb, nrows, t, e)
+                      : launch_row(s, epi, px.n, X, X, g.nyb, nrows, t.twx, e);
         T.done();
         return err;
     }
@@ -459,6 +475,7 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
     e.sch = sch;
     e.scl = scl;
     const long long nrows = (long long)g.nyb * g.nzb;
+    if (t.bl[0]) return launch_row_bluestein(s, EPI_SCALE, px.n, X, nullptr, g.nyb, nrows, t, e);
     if (use_col_kernels() && col_supported(px.n)) return launch_row(s, EPI_SCALE, px.n, X, nullptr, g.nyb, nrows, t.twx, e);
     const int rpc = rows_per_cta(px.n);
     k_rows<true, EPI_SCALE><<<(unsigned)((nrows + rpc - 1) / rpc), kThreads, rows_smem(px.n), s>>>(
