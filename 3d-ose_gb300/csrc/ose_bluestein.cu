@@ -39,6 +39,46 @@ using cols::dftc;
 
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
+// DFT-16 as dftc<16, ST> (4 x 4: DFT-4 over m of v[4 m + r], twiddle, DFT-4
+// over r), for the halves Bluestein leaves: LOW_IN = inputs v[8..15] are zero
+// (the first DFT-4s see (a, b, 0, 0)); LOW_OUT = only v[0..7] is wanted
+// (the last DFT-4s give outputs 0 and 1).  Same arithmetic on the rest.
+template <int ST, bool INV, bool LOW_IN, bool LOW_OUT>
+__device__ __forceinline__ void dft16_half(float2 (&v)[16], const float2* __restrict__ W)
+{
+    float2 t[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        if (LOW_IN) {
+            const float2 a = v[r], b = v[4 + r], rb = cols::rot<INV>(b);
+            t[r][0] = cadd(a, b);
+            t[r][1] = cadd(a, rb);
+            t[r][2] = csub(a, b);
+            t[r][3] = csub(a, rb);
+        } else {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) t[r][m] = v[4 * m + r];
+            dftc<4, ST * 4, INV, 4>(t[r], W);
+        }
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+        float2 u[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) u[r] = (r * k2) ? cmul(t[r][k2], cols::tw<INV>(W, ST * r * k2)) : t[r][k2];
+        if (LOW_OUT) {
+            const float2 t0 = cadd(u[0], u[2]), t1 = csub(u[0], u[2]), t2 = cadd(u[1], u[3]);
+            const float2 t3 = cols::rot<INV>(csub(u[1], u[3]));
+            v[k2] = cadd(t0, t2);
+            v[k2 + 4] = cadd(t1, t3);
+        } else {
+            dftc<4, ST * 4, INV, 4>(u, W);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) v[k2 + 4 * k1] = u[k1];
+        }
+    }
+}
+
 template <int C>
 struct Cfg {
     static constexpr int L = 16 * C;
@@ -82,7 +122,7 @@ __device__ __forceinline__ void bs_line(float2 (&v)[8], int p, IDX idx, float2* 
         }
 #pragma unroll
         for (int n1 = 8; n1 < 16; ++n1) w[n1] = make_float2(0.f, 0.f);
-        dftc<16, C, false>(w, W);
+        dft16_half<C, false, true, false>(w, W);
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) T[idx(p, k1)] = k1 ? cmul(w[k1], W[p * k1]) : w[k1];
     }
@@ -105,7 +145,7 @@ __device__ __forceinline__ void bs_line(float2 (&v)[8], int p, IDX idx, float2* 
     if (p < C) {
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) w[k1] = T[idx(p, k1)];
-        dftc<16, C, true>(w, W);    // w[n1] = (a * b)[C n1 + p]
+        dft16_half<C, true, false, true>(w, W);    // w[n1] = (a * b)[C n1 + p], n1 < 8
 #pragma unroll
         for (int n1 = 0; n1 < 8; ++n1) {
             const int m = C * n1 + p;
