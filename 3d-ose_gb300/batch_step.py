@@ -7,7 +7,8 @@ explicit tunings, e.g. to capture one step's launches under a profiler.
 
 run: reset, then STEPS (default 2) steps with the given shot-group size (MB of
 fields per L2-sized group, 0 = one group) and number of concurrent per-shot
-lanes (0 = batched launches).  time: the step time of a few fixed tunings.
+lanes (0 = batched launches, -1 = one persistent launch per step).  time:
+the step time of a few fixed tunings.
 """
 from __future__ import annotations
 
@@ -36,7 +37,7 @@ def main(argv):
             b.run(int(argv[5]) if len(argv) > 5 else 2)
             return 0
         out = {}
-        for g, lanes in ((0, 0), (48, 0), (96, 0), (0, 2), (0, 4)):
+        for g, lanes in ((0, 0), (48, 0), (96, 0), (0, 2), (0, 4), (0, -1), (48, -1), (96, -1)):
             b.set_tuning(group_mb=g, lanes=lanes)
             b.reset()
             b.run(3)

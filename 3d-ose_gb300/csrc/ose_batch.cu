@@ -55,8 +55,17 @@ struct ose_batch {
     // lanes = 0: batched launches (one per pass and length class).  lanes = k
     // > 0: every shot's own single-shot launches, shots spread round-robin
     // over k streams that run concurrently inside the captured step.
+    // lanes = -1: the whole step (after the source injection) as one
+    // persistent cooperative launch over the batched passes, grid barriers
+    // between passes (ose_cols.cu kb_persistent).
     int lanes = 0;
     static constexpr int kMaxLanes = 8;
+    ose::PersistPass* d_ppass = nullptr;
+    int nppass = 0;
+    size_t ppass_cap = 0;
+    bool persist_ok = false;   // every pass of the batch has a persistent kernel
+    unsigned* d_bar = nullptr; // [0] arrivals, [1] generation, [2] error word
+    int pgrid = 0;
     cudaStream_t lane[kMaxLanes] = {};
     cudaEvent_t fork = nullptr, join[kMaxLanes] = {};
     std::string err;
@@ -191,6 +200,35 @@ ose_status build_passes(ose_batch* b)
     BCK(b, cudaStreamSynchronize(b->stream));
     for (const Range& r : ranges)
         b->passes.push_back({b->d_work + r.off, (int)r.count, r.smem, r.kind, r.n_axis, r.n});
+    // the same passes for the persistent launch: a grid barrier after the
+    // last length class of every (group, application, kind)
+    b->persist_ok = !ranges.empty();
+    std::vector<ose::PersistPass> pp;
+    for (size_t i = 0; i < ranges.size(); ++i) {
+        const Range& r = ranges[i];
+        if (!ose::persist_supported(r.n_axis)) b->persist_ok = false;
+        const bool last = i + 1 == ranges.size() || ranges[i + 1].kind != r.kind || ranges[i + 1].n != r.n ||
+                          ranges[i + 1].off < r.off;
+        pp.push_back({b->d_work + r.off, (int)r.count, r.kind, r.n_axis, r.n, last ? 1 : 0});
+    }
+    // a new group restarts at application 0, kind 0: that change of (n, kind)
+    // already puts a barrier between groups
+    if (b->persist_ok) {
+        if (pp.size() > b->ppass_cap) {
+            if (b->d_ppass) cudaFree(b->d_ppass);
+            b->d_ppass = nullptr;
+            BCK(b, cudaMalloc((void**)&b->d_ppass, sizeof(ose::PersistPass) * pp.size()));
+            b->ppass_cap = pp.size();
+        }
+        BCK(b, cudaMemcpy(b->d_ppass, pp.data(), sizeof(ose::PersistPass) * pp.size(), cudaMemcpyHostToDevice));
+        b->nppass = (int)pp.size();
+        if (!b->d_bar) {
+            BCK(b, cudaMalloc((void**)&b->d_bar, 4 * sizeof(unsigned)));
+            BCK(b, cudaMemset(b->d_bar, 0, 4 * sizeof(unsigned)));
+        }
+        if (!b->pgrid) b->pgrid = ose::persist_grid();
+        if (b->pgrid <= 0) b->persist_ok = false;
+    }
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     return OSE_OK;
 }
@@ -271,6 +309,12 @@ cudaError_t enqueue_batch_step(ose_batch* b)
     if (b->lanes > 0) return enqueue_lanes(b);
     cudaError_t e = ose::launch_batch_inject(b->stream, b->d_shots, b->nshots);
     if (e != cudaSuccess) return e;
+    if (b->lanes < 0) {
+        // barrier counter back to zero (the error word stays until read)
+        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned), b->stream)) != cudaSuccess) return e;
+        return ose::launch_batch_persistent(b->stream, b->d_shots, b->d_ppass, b->nppass, b->d_bar,
+                                            reinterpret_cast<int*>(b->d_bar + 2), b->pgrid);
+    }
     for (const ose::BatchPass& p : b->passes) {
         e = p.n_axis > 0 ? ose::launch_batch_col_pass(b->stream, p.kind, p.n_axis, b->d_shots, p.work, p.nblocks, p.n)
                          : ose::launch_batch_stockham_pass(b->stream, b->d_shots, p.n, p);
@@ -309,6 +353,8 @@ void free_batch(ose_batch* b)
     }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->d_work) cudaFree(b->d_work);
+    if (b->d_ppass) cudaFree(b->d_ppass);
+    if (b->d_bar) cudaFree(b->d_bar);
     if (b->d_shots) cudaFree(b->d_shots);
     if (b->arena) cudaFree(b->arena);
     if (b->ev0) cudaEventDestroy(b->ev0);
@@ -527,6 +573,19 @@ ose_status ose_batch_reset(ose_batch* b)
     return OSE_OK;
 }
 
+// A persistent step whose grid barrier timed out leaves a nonzero error word.
+static ose_status persist_status(ose_batch* b)
+{
+    if (b->lanes >= 0 || !b->d_bar) return OSE_OK;
+    unsigned w = 0;
+    BCK(b, cudaMemcpy(&w, b->d_bar + 2, sizeof w, cudaMemcpyDeviceToHost));
+    if (w) {
+        cudaMemset(b->d_bar + 2, 0, sizeof w);
+        return bfail(b, OSE_ERR_CUDA, "persistent batched step: a grid barrier timed out");
+    }
+    return OSE_OK;
+}
+
 ose_status ose_batch_run(ose_batch* b, int nsteps)
 {
     if (!b || nsteps < 0) return OSE_ERR_INVALID;
@@ -536,7 +595,7 @@ ose_status ose_batch_run(ose_batch* b, int nsteps)
     for (int i = 0; i < nsteps; ++i) BCK(b, cudaGraphLaunch(b->graph, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
     b->it += nsteps;
-    return OSE_OK;
+    return persist_status(b);
 }
 
 ose_status ose_batch_run_timed(ose_batch* b, int nsteps, float* ms)
@@ -552,7 +611,7 @@ ose_status ose_batch_run_timed(ose_batch* b, int nsteps, float* ms)
     BCK(b, cudaEventSynchronize(b->ev1));
     BCK(b, cudaEventElapsedTime(ms, b->ev0, b->ev1));
     b->it += nsteps;
-    return OSE_OK;
+    return persist_status(b);
 }
 
 ose_status ose_batch_info(const ose_batch* b, int shot, ose_derived* d, long long* cells)
@@ -611,11 +670,12 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
                 const int nf = sscanf(line, "%32767s %d %d %d %d %d %d", key, &rs, &ty, &tz, &ro, &gm, &ln);
                 if (nf >= 5 && sig == key) {
                     b->rows_scale = rs; b->txy = ty; b->txz = tz; b->radix_order = ro; b->group_mb = gm;
-                    b->lanes = std::min(std::max(ln, 0), (int)ose_batch::kMaxLanes);
+                    b->lanes = std::min(std::max(ln, -1), (int)ose_batch::kMaxLanes);
                     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
                     fclose(f);
                     fill_descriptors(b);
                     ose_status st = build_passes(b);
+                    if (st == OSE_OK && b->lanes < 0 && !b->persist_ok) b->lanes = 0;
                     if (best_ms) *best_ms = -1.f;
                     return st != OSE_OK ? st : ose_batch_reset(b);
                 }
@@ -643,10 +703,34 @@ ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, f
         if (measure(&ms) == OSE_OK && ms < best) best = ms;
         else b->lanes = keep;
     }
+    // the persistent launch over the batched passes, with shot groups sized
+    // for L2 or one group
+    {
+        fill_descriptors(b);
+        if (build_passes(b) == OSE_OK && b->persist_ok) {
+            const int keep_l = b->lanes, keep_g = b->group_mb;
+            int best_g = -1;
+            for (int gm : {0, 96, 48}) {
+                b->lanes = -1;
+                b->group_mb = gm;
+                if (measure(&ms) == OSE_OK && ms < best) {
+                    best = ms;
+                    best_g = gm;
+                }
+            }
+            if (best_g >= 0) {
+                b->lanes = -1;
+                b->group_mb = best_g;
+            } else {
+                b->lanes = keep_l;
+                b->group_mb = keep_g;
+            }
+        }
+    }
     // then the group size of batched launches: it decides whether fields stay
     // in L2 (1 MB: one shot per group, since every shot is larger)
     for (int gm : {1024, 256, 96, 1}) {
-        if (b->lanes > 0) break;
+        if (b->lanes != 0) break;
         const int keep = b->group_mb;
         b->group_mb = gm;
         if (measure(&ms) == OSE_OK && ms < best) best = ms;
@@ -694,7 +778,7 @@ ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, 
                                 int lanes)
 {
     if (!b || rows_scale < 1 || txy < 1 || txz < 1 || radix_order < 0 || radix_order > 1 || group_mb < 0 ||
-        lanes < 0 || lanes > ose_batch::kMaxLanes)
+        lanes < -1 || lanes > ose_batch::kMaxLanes)
         return OSE_ERR_INVALID;
     b->lanes = lanes;
     b->rows_scale = rows_scale;
@@ -704,7 +788,13 @@ ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, 
     b->group_mb = group_mb;
     fill_descriptors(b);
     ose_status st = build_passes(b);
-    return st != OSE_OK ? st : ose_batch_reset(b);
+    if (st != OSE_OK) return st;
+    if (lanes < 0 && !b->persist_ok) {
+        b->lanes = 0;
+        return bfail(b, OSE_ERR_UNSUPPORTED, "the persistent step needs axis lengths 16 C with C <= 16 and a "
+                                             "cooperative launch");
+    }
+    return ose_batch_reset(b);
 }
 
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,

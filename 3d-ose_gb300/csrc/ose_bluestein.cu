@@ -326,11 +326,14 @@ cudaError_t launch_row_c(cudaStream_t s, int epi, int n, const float2* src, floa
 
 // Bluestein length for an axis of length n: the smallest L = 16 C, C in the
 // instantiated set, with L >= 2 n - 1; 0 = the axis keeps its own kernels
-// (a register four-step length, longer than 192, or no prime factor >= 11,
-// where the Stockham radices 2..7 already serve it).
+// (a register four-step length, shorter than 128 — where the Stockham
+// stages, paired direct DFTs included, cost little — longer than 192, or no
+// prime factor >= 11, where the Stockham radices 2..7 already serve it).
+// The batched form has no Bluestein kernels: its shots keep the Stockham
+// passes on such lengths.
 int bluestein_length(int n)
 {
-    if (n < 2 || n > 192 || col_supported(n)) return 0;
+    if (n < 128 || n > 192 || col_supported(n)) return 0;
     int t = n, big = 1;
     for (int f = 2; f <= t; ++f)
         while (t % f == 0) { t /= f; big = f; }

@@ -15,6 +15,8 @@
 // the step's pointwise epilogue.  These replace the shared-memory Stockham
 // passes (ose_kernels.cu) on these sizes.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "ose_dft.cuh"
@@ -40,7 +42,8 @@ struct ColCfg {
 // Lines at base + n * stride of the columns x0 .. x0 + TX - 1 (x tile xt);
 // `other` = the other index (z for the y passes, y for the z pass).
 // W: shared twiddle table (N), T: shared transpose buffer (N x TX).
-template <int C, int MODE>
+// COHERENT: column loads bypass the SM's L1 (as row_body's).
+template <int C, int MODE, bool COHERENT = false>
 __device__ __forceinline__ void col_body(float2* __restrict__ X, int nxb, long long stride, long long ostride,
                                          const float2* __restrict__ twg, const float* __restrict__ kx2,
                                          const float* __restrict__ ky2, const float* __restrict__ kz2, int xt,
@@ -59,7 +62,10 @@ __device__ __forceinline__ void col_body(float2* __restrict__ X, int nxb, long l
         if (p < C) {   // phase 1: thread j = p, DFT-16 over n1
             float2 v[16];
 #pragma unroll
-            for (int n1 = 0; n1 < 16; ++n1) v[n1] = col_ok ? line[(size_t)(C * n1 + p) * stride] : make_float2(0.f, 0.f);
+            for (int n1 = 0; n1 < 16; ++n1) {
+                const float2* a = line + (size_t)(C * n1 + p) * stride;
+                v[n1] = col_ok ? (COHERENT ? __ldcg(a) : *a) : make_float2(0.f, 0.f);
+            }
             dftc<16, C, false>(v, W);
 #pragma unroll
             for (int k1 = 0; k1 < 16; ++k1) T[(p * 16 + k1) * TX + c] = k1 ? cmul(v[k1], W[p * k1]) : v[k1];
@@ -70,7 +76,10 @@ __device__ __forceinline__ void col_body(float2* __restrict__ X, int nxb, long l
     if (p < 16) {
         if (MODE == COL_INV) {
 #pragma unroll
-            for (int k2 = 0; k2 < C; ++k2) u[k2] = col_ok ? line[(size_t)(p + 16 * k2) * stride] : make_float2(0.f, 0.f);
+            for (int k2 = 0; k2 < C; ++k2) {
+                const float2* a = line + (size_t)(p + 16 * k2) * stride;
+                u[k2] = col_ok ? (COHERENT ? __ldcg(a) : *a) : make_float2(0.f, 0.f);
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < C; ++j) u[j] = T[(j * 16 + p) * TX + c];
@@ -125,21 +134,27 @@ __global__ void __launch_bounds__(ColCfg<C>::THREADS, ColCfg<C>::MINB) k_col(flo
 
 // Batched: CTA b works on block work[b].y = x tile + (x tiles) * other of
 // shot work[b].x; AXIS 1 = y lines, 2 = z lines.
-template <int C, int MODE, int AXIS>
-__global__ void __launch_bounds__(ColCfg<C>::THREADS, ColCfg<C>::MINB) kb_col(const BatchShot* __restrict__ shots,
-                                                             const int2* __restrict__ work)
+template <int C, int MODE, int AXIS, bool COHERENT = false>
+__device__ __forceinline__ void kb_col_item(const BatchShot* __restrict__ shots, int2 wk, float2* W)
 {
-    extern __shared__ float4 smem4[];
-    float2* W = reinterpret_cast<float2*>(smem4);
-    const int2 wk = work[blockIdx.x];
     const BatchShot& S = shots[wk.x];
     const int ntx = (S.g.nxb + ColCfg<C>::TX - 1) / ColCfg<C>::TX;
     const int xt = wk.y % ntx, other = wk.y / ntx;
     const long long plane = (long long)S.g.nxb * S.g.nyb;
     if (AXIS == 1)
-        col_body<C, MODE>(S.X, S.g.nxb, S.g.nxb, plane, S.twy, S.kx2, S.ky2, S.kz2, xt, other, W, W + ColCfg<C>::N);
+        col_body<C, MODE, COHERENT>(S.X, S.g.nxb, S.g.nxb, plane, S.twy, S.kx2, S.ky2, S.kz2, xt, other, W,
+                                    W + ColCfg<C>::N);
     else
-        col_body<C, MODE>(S.X, S.g.nxb, plane, S.g.nxb, S.twz, S.kx2, S.ky2, S.kz2, xt, other, W, W + ColCfg<C>::N);
+        col_body<C, MODE, COHERENT>(S.X, S.g.nxb, plane, S.g.nxb, S.twz, S.kx2, S.ky2, S.kz2, xt, other, W,
+                                    W + ColCfg<C>::N);
+}
+
+template <int C, int MODE, int AXIS>
+__global__ void __launch_bounds__(ColCfg<C>::THREADS, ColCfg<C>::MINB) kb_col(const BatchShot* __restrict__ shots,
+                                                             const int2* __restrict__ work)
+{
+    extern __shared__ float4 smem4[];
+    kb_col_item<C, MODE, AXIS>(shots, work[blockIdx.x], reinterpret_cast<float2*>(smem4));
 }
 
 template <int C>
@@ -157,7 +172,9 @@ struct RowCfg {
 // epilogue<EPI>; FWD (FIRST, MID): then the forward transform of the new term
 // a_{n+1}, still in registers, into dst (the next application's x pass; each
 // row is read before it is written, by the same CTA).
-template <int C, int EPI, bool FWD = false>
+// COHERENT: the rows are read with loads that bypass the SM's L1 (the
+// persistent kernel reads fields other CTAs wrote earlier in the same launch).
+template <int C, int EPI, bool FWD = false, bool COHERENT = false>
 __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2* __restrict__ dst, int nyb,
                                          long long nrows, const float2* __restrict__ twg, const EpiArgs& e,
                                          long long rb, float2* W, float2* T)
@@ -175,7 +192,8 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
             float2 v[16];
             const float2* in = src + row * N + q;
 #pragma unroll
-            for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? in[C * n1] : make_float2(0.f, 0.f);
+            for (int n1 = 0; n1 < 16; ++n1)
+                v[n1] = ok ? (COHERENT ? __ldcg(in + C * n1) : in[C * n1]) : make_float2(0.f, 0.f);
             dftc<16, C, false>(v, W);
 #pragma unroll
             for (int k1 = 0; k1 < 16; ++k1) Tr[q * 17 + k1] = k1 ? cmul(v[k1], W[q * k1]) : v[k1];
@@ -195,7 +213,8 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
             float2 u[C];
             const float2* in = src + row * N + q;
 #pragma unroll
-            for (int k2 = 0; k2 < C; ++k2) u[k2] = ok ? in[16 * k2] : make_float2(0.f, 0.f);
+            for (int k2 = 0; k2 < C; ++k2)
+                u[k2] = ok ? (COHERENT ? __ldcg(in + 16 * k2) : in[16 * k2]) : make_float2(0.f, 0.f);
             dftc<C, 16, true>(u, W);
 #pragma unroll
             for (int j = 0; j < C; ++j) {
@@ -210,7 +229,7 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
             for (int k1 = 0; k1 < 16; ++k1) v[k1] = Tr[q * 17 + k1];
             dftc<16, C, true>(v, W);
             const int y = (int)(row % nyb), z = (int)(row / nyb);
-            epilogue_row<EPI, 16, FWD>(v, row * N + q, q, C, y, z, e);
+            epilogue_row<EPI, 16, FWD, COHERENT>(v, row * N + q, q, C, y, z, e);
             if (FWD) {   // forward phase 1 of a_{n+1} (v[n1] = a[C n1 + j]); thread q owns Tr row q
                 dftc<16, C, false>(v, W);
 #pragma unroll
@@ -244,25 +263,116 @@ __global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __rest
 
 // Batched x rows of application n: forward (a_n -> X) or inverse + the series
 // update (FIRST, MID or LAST by the shot's series order M).
+template <int C, bool INV, bool COHERENT = false>
+__device__ __forceinline__ void kb_row_item(const BatchShot* __restrict__ shots, int2 wk, int n, float2* W)
+{
+    float2* T = W + RowCfg<C>::N;
+    const BatchShot& S = shots[wk.x];
+    const long long nrows = (long long)S.g.nyb * S.g.nzb;
+    if (!INV) {
+        const float2* src = n == 0 ? S.W : ((n & 1) ? S.A : S.W);
+        row_body<C, EPI_NONE, false, COHERENT>(src, S.X, S.g.nyb, nrows, S.twx, EpiArgs{}, wk.y, W, T);
+        return;
+    }
+    const EpiArgs e = batch_epi(S, n);
+    if (n == 0) row_body<C, EPI_FIRST, false, COHERENT>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+    else if (n == S.M) row_body<C, EPI_LAST, false, COHERENT>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+    else row_body<C, EPI_MID, false, COHERENT>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+}
+
 template <int C, bool INV>
 __global__ void __launch_bounds__(RowCfg<C>::THREADS) kb_row(const BatchShot* __restrict__ shots,
                                                              const int2* __restrict__ work, int n)
 {
     extern __shared__ float4 smem4[];
-    float2* W = reinterpret_cast<float2*>(smem4);
-    float2* T = W + RowCfg<C>::N;
-    const int2 wk = work[blockIdx.x];
-    const BatchShot& S = shots[wk.x];
-    const long long nrows = (long long)S.g.nyb * S.g.nzb;
-    if (!INV) {
-        const float2* src = n == 0 ? S.W : ((n & 1) ? S.A : S.W);
-        row_body<C, EPI_NONE>(src, S.X, S.g.nyb, nrows, S.twx, EpiArgs{}, wk.y, W, T);
-        return;
+    kb_row_item<C, INV>(shots, work[blockIdx.x], n, reinterpret_cast<float2*>(smem4));
+}
+
+// ---- the batched step as one persistent cooperative launch ----
+//
+// Every CTA walks the same list of phases (the batched passes in launch
+// order: per shot group, application and pass kind, one entry per axis-length
+// class); inside a phase it takes work items (shot, block) strided by the
+// grid, and between phases all CTAs meet at a grid barrier.  Only lengths
+// 16 C with C <= 16 take part (their row and column kernels all have 256
+// threads).  The barrier is a counter and a generation word in global
+// memory; a CTA waits at most kBarrierLimitNs for the others, then sets
+// *err and leaves the kernel, so a failed step ends instead of hanging.
+constexpr int kPersistThreads = 256;
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long now_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// bar[0] = arrivals, bar[1] = generation.  Returns false after a timeout.
+__device__ bool grid_barrier(unsigned* bar, int* err)
+{
+    __syncthreads();
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const unsigned long long t0 = now_ns();
+            while (*gen == g) {
+                if (now_ns() - t0 > kBarrierLimitNs) {
+                    ok = 0;
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
     }
-    const EpiArgs e = batch_epi(S, n);
-    if (n == 0) row_body<C, EPI_FIRST>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
-    else if (n == S.M) row_body<C, EPI_LAST>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
-    else row_body<C, EPI_MID>(S.X, nullptr, S.g.nyb, nrows, S.twx, e, wk.y, W, T);
+    const bool all = __syncthreads_and(ok) != 0;
+    __threadfence();   // every thread orders its later loads after the barrier
+    return all;
+}
+
+template <int C>
+__device__ __forceinline__ void persist_item(const BatchShot* shots, int kind, int2 wk, int n, float2* W)
+{
+    switch (kind) {
+    case 0: kb_row_item<C, false, true>(shots, wk, n, W); break;
+    case 1: kb_col_item<C, COL_FWD, 1, true>(shots, wk, W); break;
+    case 2: kb_col_item<C, COL_KSCALE, 2, true>(shots, wk, W); break;
+    case 3: kb_col_item<C, COL_INV, 1, true>(shots, wk, W); break;
+    default: kb_row_item<C, true, true>(shots, wk, n, W); break;
+    }
+}
+
+#define OSE_PERSIST_SIZES(X) X(4) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(16)
+
+__global__ void __launch_bounds__(kPersistThreads, 2) kb_persistent(const BatchShot* __restrict__ shots,
+                                                                    const PersistPass* __restrict__ passes,
+                                                                    int npass, unsigned* bar, int* err)
+{
+    extern __shared__ float4 smem4[];
+    float2* W = reinterpret_cast<float2*>(smem4);
+    for (int pi = 0; pi < npass; ++pi) {
+        const PersistPass P = passes[pi];
+        for (int w = blockIdx.x; w < P.nblocks; w += gridDim.x) {
+            const int2 wk = P.work[w];
+            switch (P.n_axis / 16) {
+#define ITEM(C) case C: persist_item<C>(shots, P.kind, wk, P.n, W); break;
+                OSE_PERSIST_SIZES(ITEM)
+#undef ITEM
+            default: break;
+            }
+            __syncthreads();   // the next item overwrites the twiddle table and the transpose buffer
+        }
+        if (P.barrier_after && !grid_barrier(bar, err)) return;
+    }
 }
 
 template <int C, int EPI, bool FWD = false>
@@ -369,6 +479,56 @@ cudaError_t launch_batch_col_pass(cudaStream_t s, int kind, int n_axis, const Ba
 #undef LAUNCH
     default: return cudaErrorInvalidValue;
     }
+}
+
+bool persist_supported(int n_axis)
+{
+    switch (n_axis / 16) {
+#define CASE(C) case C:
+        OSE_PERSIST_SIZES(CASE)
+#undef CASE
+        return n_axis % 16 == 0;
+    default: return false;
+    }
+}
+
+size_t persist_smem()
+{
+    size_t m = 0;
+#define SM(C) m = std::max(m, std::max(cols::ColCfg<C>::SMEM, cols::RowCfg<C>::SMEM));
+    OSE_PERSIST_SIZES(SM)
+#undef SM
+    return m;
+}
+
+int persist_grid()
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaFuncSetAttribute(cols::kb_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)persist_smem()) !=
+        cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cols::kb_persistent, cols::kPersistThreads,
+                                                      persist_smem()) != cudaSuccess)
+        return 0;
+    return sms * per;
+}
+
+cudaError_t launch_batch_persistent(cudaStream_t s, const BatchShot* shots, const PersistPass* passes, int npass,
+                                    unsigned* bar, int* err, int grid)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(cols::kPersistThreads);
+    cfg.dynamicSmemBytes = persist_smem();
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, cols::kb_persistent, shots, passes, npass, bar, err);
 }
 
 int col_tile(int n_axis) { return n_axis / 16 > 16 ? 8 : 16; }

@@ -87,7 +87,9 @@ __device__ __forceinline__ void epilogue(long long i, int x, int y, int z, float
 // KEEP (FIRST, MID): v also receives the new term a_{n+1}, for the next
 // application's forward transform in the same kernel.  Only the first
 // `valid` cells exist (a row shorter than CNT * xs); the others are left alone.
-template <int EPI, int CNT, bool KEEP = false>
+// COH: a_{n-1} and S are read with loads that bypass the SM's L1 (for a
+// persistent kernel that reads fields other CTAs wrote in the same launch).
+template <int EPI, int CNT, bool KEEP = false, bool COH = false>
 __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int x0, int xs, int y, int z,
                                              const EpiArgs& e, int valid = CNT)
 {
@@ -104,8 +106,8 @@ __device__ __forceinline__ void epilogue_row(float2 (&v)[CNT], long long i0, int
             if (k >= valid) continue;
             vv[q] = __ldg(e.vs + i);
             if (EPI == EPI_MID || EPI == EPI_LAST) {
-                am[q] = e.prev[i];
-                sm[q] = e.sp.s_read ? e.S[i] : make_float2(0.f, 0.f);
+                am[q] = COH ? __ldcg(e.prev + i) : e.prev[i];
+                sm[q] = e.sp.s_read ? (COH ? __ldcg(e.S + i) : e.S[i]) : make_float2(0.f, 0.f);
                 axv[q] = e.sp.touch ? __ldg(e.ax + x0 + k * xs) : 1.f;
             }
         }

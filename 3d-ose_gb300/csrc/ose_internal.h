@@ -307,6 +307,23 @@ struct BatchPass {
 };
 
 cudaError_t configure_batch_kernels();
+
+// The batched step as one persistent cooperative launch (ose_cols.cu): one
+// entry per batched pass in launch order; barrier_after = the grid meets
+// before the next entry (after the last length class of a pass).
+struct PersistPass {
+    const int2* work;
+    int nblocks;
+    int kind;
+    int n_axis;
+    int n;
+    int barrier_after;
+};
+bool persist_supported(int n_axis);
+size_t persist_smem();
+int persist_grid();   // CTAs of a co-resident grid on the current device (0 = unavailable)
+cudaError_t launch_batch_persistent(cudaStream_t s, const BatchShot* shots, const PersistPass* passes, int npass,
+                                    unsigned* bar, int* err, int grid);
 cudaError_t launch_batch_inject(cudaStream_t s, const BatchShot* shots, int nshots);
 // One pass of operator application n (shared-memory Stockham kernels).
 cudaError_t launch_batch_stockham_pass(cudaStream_t s, const BatchShot* shots, int n, const BatchPass& p);

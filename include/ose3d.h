@@ -373,7 +373,11 @@ ose_status ose_batch_get_gather(ose_batch* b, int shot, float* out);
 ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out);
 /* Pick the batching strategy (lanes = 0: one batched launch per pass and axis
  * length for all shots; lanes = k > 0: every shot's single-shot launches,
- * shots spread over k streams that run concurrently in the captured step),
+ * shots spread over k streams that run concurrently in the captured step;
+ * lanes = -1: the source injection and then ONE persistent cooperative
+ * launch per step that runs every batched pass, with grid barriers between
+ * passes — available when every axis length is 16 C with C <= 16; a barrier
+ * that waits longer than 2 s ends the step with OSE_ERR_CUDA),
  * the shot grouping of batched launches (groups whose working set stays
  * within group_mb MB, so a group's fields can stay in L2 through its step;
  * 0 = all shots together) and, for axis lengths without register kernels, the rows
@@ -384,8 +388,9 @@ ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out
 ose_status ose_batch_autotune(ose_batch* b, int steps, const char* cache_path, float* best_ms);
 ose_status ose_batch_get_tuning(const ose_batch* b, int* rows_scale, int* txy, int* txz, int* radix_order,
                                 int* group_mb, int* lanes);
-/* Set the tuning by hand (the values ose_batch_get_tuning returns; lanes <= 8).
- * Resets the batch. */
+/* Set the tuning by hand (the values ose_batch_get_tuning returns; -1 <= lanes
+ * <= 8; OSE_ERR_UNSUPPORTED for lanes = -1 on a batch without the persistent
+ * form).  Resets the batch. */
 ose_status ose_batch_set_tuning(ose_batch* b, int rows_scale, int txy, int txz, int radix_order, int group_mb,
                                 int lanes);
 

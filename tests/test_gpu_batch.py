@@ -103,3 +103,37 @@ def test_register_classes_and_lanes_match_single_shots(lanes):
                 g = h.run(BASE["nt"], want_gather=True)
                 assert np.array_equal(b.gather(s), g)
                 assert np.array_equal(b.wavefield(s, ose3d.FIELD_Q), h.wavefield(ose3d.FIELD_Q))
+
+
+# padded 64^3, 96 x 64 x 112 and 64 x 96 x 64: every axis 16 C with C <= 16
+PERSIST_WINDOWS = [dict(x0=0, y0=0, z0=0, nx=52, ny=52, nz=52, sx=20, sy=26, sz=3),
+                   dict(x0=8, y0=4, z0=0, nx=84, ny=52, nz=100, sx=40, sy=20, sz=2),
+                   dict(x0=20, y0=10, z0=2, nx=52, ny=84, nz=52, sx=30, sy=40, sz=5)]
+
+
+@pytest.mark.parametrize("group_mb", [0, 1])
+def test_persistent_step_matches_single_shots(group_mb):
+    """The whole batched step as one persistent cooperative launch (grid
+    barriers between the passes), all shots in one group or one shot per
+    group: bit for bit the single-shot handles."""
+    m = model(seed=11, shape=(100, 100, 110))
+    p = ose3d.default_params(**BASE)
+    with ose3d.Batch(p, m, PERSIST_WINDOWS) as b:
+        b.set_tuning(lanes=-1, group_mb=group_mb)
+        assert b.tuning()["lanes"] == -1
+        b.run(BASE["nt"])
+        for s, w in enumerate(PERSIST_WINDOWS):
+            with single(m, w) as h:
+                h.reset_shot(0)
+                g = h.run(BASE["nt"], want_gather=True)
+                assert np.array_equal(b.gather(s), g)
+                assert np.array_equal(b.wavefield(s, ose3d.FIELD_Q), h.wavefield(ose3d.FIELD_Q))
+                assert np.array_equal(b.wavefield(s, ose3d.FIELD_P), h.wavefield(ose3d.FIELD_P))
+
+
+def test_persistent_step_refused_where_a_length_has_no_kernel():
+    m = model(seed=9, shape=(100, 100, 60))
+    with ose3d.Batch(ose3d.default_params(**BASE), m, REG_WINDOWS) as b:   # a 48-long axis
+        with pytest.raises(ose3d.OseError):
+            b.set_tuning(lanes=-1)
+        assert b.tuning()["lanes"] == 0
