@@ -332,7 +332,8 @@ ose_status build_graph(ose_handle* h)
 ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVALID; }
 
 // After the stream is idle: kernels with bounded waits (tensor-core z pass,
-// corrector) record a wait that ran out of time in the handle's error word.
+// corrector, the plane kernels' exchanges) record a wait that ran out of time
+// in the handle's error word.
 ose_status tensor_status(ose_handle* h)
 {
     if (!h->tcerr) return OSE_OK;
@@ -340,8 +341,9 @@ ose_status tensor_status(ose_handle* h)
     CK(h, cudaMemcpy(&v, h->tcerr, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
         CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
-        return fail(h, OSE_ERR_CUDA, v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
-                                            : "tensor-core z pass: an MMA completion wait ran out of time");
+        return fail(h, OSE_ERR_CUDA, v == 3   ? "plane kernels: a DSMEM exchange wait ran out of time"
+                                     : v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
+                                              : "tensor-core z pass: an MMA completion wait ran out of time");
     }
     return OSE_OK;
 }

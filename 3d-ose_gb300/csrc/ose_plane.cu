@@ -14,7 +14,13 @@
 // Plane work is split over the cluster: CTA r owns rows y in [32r, 32r+32) for
 // the x transforms and columns x in [32r, 32r+32) for the y transforms; the
 // 512 KiB plane changes hands between the two through distributed shared
-// memory (each CTA's 64 KiB slice, read by the others with ld.shared::cluster).
+// memory: each CTA pushes the 32 x 32 blocks it holds into their owners'
+// receive buffers with st.async, whose bytes complete a transaction count on
+// the receiver's mbarrier, so a receiver waits on its own barrier and no
+// cluster-scope release (which would also wait for every global store in
+// flight, such as the epilogue's) is needed.  One relaxed cluster barrier per
+// exchange tells the senders that the receive buffers (which overlay the
+// transpose buffer) are free.
 //
 // Every 256-point transform is a four-step 16 x 16 FFT: a line is held by 16
 // threads with 16 values each, a radix-16 DFT runs in registers, twiddles
@@ -28,6 +34,7 @@
 #include "ose_internal.h"
 #include "ose_epilogue.cuh"
 #include "ose_pdl.cuh"
+#include "tcgen05.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -58,7 +65,8 @@ constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange 
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
 // + twiddle table (hi, lo) + the x sponge factor's powers ax, ax^2, ax^3 (3 N floats)
 constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N + 3 * N / 2;
-constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX;
+// + the exchange's mbarrier
+constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX + 16;
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -155,6 +163,106 @@ __device__ __forceinline__ void dft16(float2 (&v)[16])
     t = v[11]; v[11] = v[14]; v[14] = t;
 }
 
+#ifndef OSE_PLANE_PUSH
+#define OSE_PLANE_PUSH 1
+#endif
+constexpr bool PUSH = OSE_PLANE_PUSH != 0;
+// bytes each CTA receives per exchange: a 32 x 32 block from each other CTA
+constexpr unsigned PUSH_BYTES = (CL - 1) * SL * SL * sizeof(float2);
+constexpr uint64_t PUSH_WAIT_NS = 2000000000ull;   // then the error word is set
+constexpr int ERR_PLANE_EXCHANGE = 3;
+
+__device__ __forceinline__ void cluster_arrive_relaxed()
+{
+    asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait;" ::: "memory"); }
+
+// The shared::cluster address of shared-memory address a in CTA `rank`.
+__device__ __forceinline__ uint32_t map_rank(uint32_t a, int rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+
+// 8 bytes into another CTA's shared memory; completes 8 transaction bytes on
+// that CTA's barrier.
+__device__ __forceinline__ void push8(uint32_t addr, float2 v, uint32_t bar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
+                 "f"(v.x), "f"(v.y), "r"(bar)
+                 : "memory");
+}
+
+// Waits for the phase with the given parity to complete, with acquire
+// semantics at cluster scope (the bytes come from other CTAs' st.async);
+// false after limit_ns nanoseconds.
+__device__ __forceinline__ bool wait_pushed(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
+{
+    const uint32_t a = tc5::smem_u32(bar);
+    uint64_t t0 = 0;
+    for (bool first = true;; first = false) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (first) t0 = tc5::global_ns();
+        else if (tc5::global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// Receiving side of the exchanges of one kernel: the mbarrier (one arrival,
+// by thread 0 with the expected bytes, per exchange), the phase, and whether
+// every wait so far completed.
+struct Exchange {
+    uint64_t* bar;
+    int* err;
+    uint32_t phase;
+    bool ok;
+};
+
+__device__ __forceinline__ void arm(uint64_t* bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     tc5::smem_u32(bar)),
+                 "r"(PUSH_BYTES)
+                 : "memory");
+}
+
+// Thread 0 initialises the barrier and arms the first exchange; the other
+// CTAs see the initialisation through the relaxed cluster barrier that comes
+// before any push.
+__device__ __forceinline__ Exchange exchange_init(float2* smem, int* err)
+{
+    Exchange x{reinterpret_cast<uint64_t*>(smem + SMEM_COMPLEX), err, 0u, true};
+    if (PUSH && threadIdx.x == 0) {
+        tc5::mbar_init(x.bar, 1);
+        arm(x.bar);
+    }
+    return x;
+}
+
+// Waits (bounded) until every pushed block of this exchange has landed, arms
+// the next exchange (more) and makes this CTA's own block, written with plain
+// stores, visible to all its threads.  A wait that runs out of time sets the
+// error word; the kernel still passes every later barrier, so nothing hangs.
+__device__ __forceinline__ void receive(Exchange& x, bool more)
+{
+    if (x.ok && !wait_pushed(x.bar, x.phase & 1u, PUSH_WAIT_NS)) {
+        x.ok = false;
+        if (x.err) atomicExch(x.err, ERR_PLANE_EXCHANGE);
+    }
+    ++x.phase;
+    if (more && x.ok && threadIdx.x == 0) arm(x.bar);
+    __syncthreads();
+}
+
 // Rows context (x transforms): slot s of thread t handles row
 // (warp + WARPS s) * 2 + lane / 16 and line thread j = lane % 16.
 struct RowSlot {
@@ -212,8 +320,11 @@ __device__ __forceinline__ void exchange(float2* T, float2 (&v0)[16], float2 (&v
 }
 
 // Four-step 256-point transform.  Forward: v[n1] = x[16 n1 + j] in,
-// v[k2] = X[j + 16 k2] out.  Inverse: the reverse.
-template <bool INV, bool ROWS>
+// v[k2] = X[j + 16 k2] out.  Inverse: the reverse.  LOCAL_IN: v0/v1 were
+// read from a receive buffer that T overlays, so all threads finish reading
+// before T is written.  ARRIVE: arrive (relaxed) at the cluster barrier once
+// this CTA's reads of T are done, so the other CTAs may push into it.
+template <bool INV, bool ROWS, bool LOCAL_IN = false, bool ARRIVE = false>
 __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)[16], float2 (&v1)[16])
 {
 #pragma unroll
@@ -224,7 +335,9 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
 #pragma unroll
         for (int k = 1; k < 16; ++k) v[k] = cmul_ff<INV>(v[k], tw[j * k], tw[N + j * k]);
     }
+    if (LOCAL_IN) __syncthreads();
     exchange<ROWS>(T, v0, v1);
+    if (ARRIVE) cluster_arrive_relaxed();
     dft16<INV>(v0);
     if (NS > 1) dft16<INV>(v1);
 }
@@ -237,6 +350,7 @@ struct Args {
     const float* kx2;
     const float* ky2;
     const float* kz2;
+    int* err;              // error word (an exchange wait that ran out of time)
     EpiArgs e;
 };
 
@@ -256,12 +370,68 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Columns to rows: this CTA (columns x in [32r, 32r+32)) sends the value at
+// (y = 16 n1 + j, x = 32 r + c) to the owner of row y, R[(y & 31) N + x].
+__device__ __forceinline__ void push_cols_to_rows(float2* R, const Exchange& xc, float2 (&v0)[16],
+                                                  float2 (&v1)[16], int r)
+{
+    const uint32_t rb = tc5::smem_u32(R), bar = tc5::smem_u32(xc.bar);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const ColSlot q = col_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+        for (int n1 = 0; n1 < 16; ++n1) {
+            const int d = n1 >> 1;
+            const int off = (16 * (n1 & 1) + q.j) * N + SL * r + q.c;
+            if (d == r) R[off] = v[n1];
+            else push8(map_rank(rb + 8u * off, d), v[n1], map_rank(bar, d));
+        }
+    }
+}
+
+// Rows to columns: this CTA (rows y in [32r, 32r+32)) sends the value at
+// (y = 32 r + row, x = j + 16 k2) to the owner of column x, R[y 32 + (x & 31)].
+__device__ __forceinline__ void push_rows_to_cols(float2* R, const Exchange& xc, float2 (&v0)[16],
+                                                  float2 (&v1)[16], int r)
+{
+    const uint32_t rb = tc5::smem_u32(R), bar = tc5::smem_u32(xc.bar);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const RowSlot q = row_slot(s);
+        float2(&v)[16] = s ? v1 : v0;
+        const int y = SL * r + q.row;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const int d = k2 >> 1;
+            const int off = y * SL + q.j + 16 * (k2 & 1);
+            if (d == r) R[off] = v[k2];
+            else push8(map_rank(rb + 8u * off, d), v[k2], map_rank(bar, d));
+        }
+    }
+}
+
 // Forward x FFT of this CTA's 32 rows (values in v0/v1, spatial order) then
 // forward y FFT of its 32 columns; spectrum stored to dst plane z.
 __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* smem, const float2* tw,
-                                           float2 (&v0)[16], float2 (&v1)[16], float2* dst, int z, int r)
+                                           float2 (&v0)[16], float2 (&v1)[16], float2* dst, int z, int r,
+                                           Exchange& xc)
 {
     float2* T = smem;
+    if (PUSH) {
+        fft256<false, true, false, true>(T, tw, v0, v1);
+        cluster_wait();   // every CTA's transpose buffer is free
+        push_rows_to_cols(smem, xc, v0, v1, r);
+        receive(xc, false);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const ColSlot q = col_slot(s);
+            float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+            for (int n1 = 0; n1 < 16; ++n1) v[n1] = smem[(16 * n1 + q.j) * SL + q.c];
+        }
+        fft256<false, false, true>(T, tw, v0, v1);
+    } else {
     fft256<false, true>(T, tw, v0, v1);
     // natural-order rows into this CTA's slice A[row][kx]
     float2* A = smem;
@@ -286,6 +456,7 @@ __device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* s
     }
     cluster.sync();
     fft256<false, false>(T, tw, v0, v1);
+    }
     float2* out = dst + (size_t)z * N * N + SL * r;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -305,6 +476,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     const int r = (int)cluster.block_rank();
     const int z = blockIdx.y;
     load_twiddles(tw, a.tw, a.twl);
+    Exchange xc = exchange_init(smem, a.err);
     griddep_launch();
     griddep_wait();
     float2 v0[16], v1[16];
@@ -317,7 +489,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
         for (int n1 = 0; n1 < 16; ++n1) v[n1] = in[(size_t)q.row * N + 16 * n1 + q.j];
     }
     __syncthreads();
-    forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
+    forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r, xc);
 }
 
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
@@ -447,6 +619,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     const size_t row0 = ((size_t)z * N + SL * r) * N;
     if (threadIdx.x == 0 && EPI != EPI_SCALE) prefetch_l2(a.e.vs + row0, SL * N * sizeof(float));
     load_twiddles(tw, a.tw, a.twl);
+    Exchange xc = exchange_init(smem, a.err);
     griddep_launch();
     griddep_wait();
     if (threadIdx.x == 0 && EPI != EPI_SCALE && EPI != EPI_FIRST) {
@@ -465,6 +638,21 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     }
     __syncthreads();
     float2* T = smem;
+    if (PUSH) {
+        fft256<true, false, false, true>(T, tw, v0, v1);
+        cluster_wait();   // every CTA's transpose buffer is free
+        push_cols_to_rows(smem, xc, v0, v1, r);
+        receive(xc, FWD);
+        // rows 32r..: thread (row, j) takes kx = j + 16 k2
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const RowSlot q = row_slot(s);
+            float2(&v)[16] = s ? v1 : v0;
+#pragma unroll
+            for (int k2 = 0; k2 < 16; ++k2) v[k2] = smem[q.row * N + q.j + 16 * k2];
+        }
+        fft256<true, true, true>(T, tw, v0, v1);
+    } else {
     fft256<true, false>(T, tw, v0, v1);
     // columns into this CTA's slice A[y][c]
     float2* A = smem;
@@ -490,10 +678,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     }
     cluster.sync();
     fft256<true, true>(T, tw, v0, v1);
+    }
     // pointwise update on (x = 16 n1 + j, y, z)
     epilogue_slot<EPI, SUM>(v0, a.e, axp, SL * r + row_slot(0).row, z, row_slot(0).j);
     if (NS > 1) epilogue_slot<EPI, SUM>(v1, a.e, axp, SL * r + row_slot(1).row, z, row_slot(1).j);
-    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r);
+    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r, xc);
 }
 
 // z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
@@ -628,6 +817,7 @@ cudaError_t launch_plane_fwd(cudaStream_t s, const float2* state, float2* X, con
     a.dst = X;
     a.tw = t.twx;
     a.twl = t.twl;
+    a.err = t.tcerr;
     return launch_pdl(plane::k_plane_fwd, dim3(plane::CL, plane::N), dim3(plane::THREADS), plane::SMEM_BYTES, s, a);
 }
 
@@ -663,6 +853,7 @@ cudaError_t launch_plane_inv(cudaStream_t s, EpiMode mode, bool fwd, const float
     a.dst = Xout;
     a.tw = t.twx;
     a.twl = t.twl;
+    a.err = t.tcerr;
     a.e = e;
     const dim3 grid(plane::CL, plane::N), block(plane::THREADS);
     const size_t sm = plane::SMEM_BYTES;
@@ -694,6 +885,7 @@ cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2
     a.src = X;
     a.tw = t.twx;
     a.twl = t.twl;
+    a.err = t.tcerr;
     a.e.prev = out;
     a.e.vs = vs;
     a.e.sch = sch;
