@@ -25,8 +25,37 @@ __host__ __device__ constexpr int first_factor(int n)
     return n;
 }
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#ifndef OSE_PACKED
+#define OSE_PACKED 1
+#endif
+// With OSE_PACKED a complex add or subtract is one packed two-lane FP32
+// instruction (add/sub.rn.f32x2: the same IEEE results as two scalar ones).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+    if (OSE_PACKED) {
+        unsigned long long d, x, y;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
+        float2 r;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+        return r;
+    }
+    return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    if (OSE_PACKED) {
+        unsigned long long d, x, y;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
+        float2 r;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+        return r;
+    }
+    return make_float2(a.x - b.x, a.y - b.y);
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
@@ -62,8 +91,9 @@ __device__ __forceinline__ void dftc(float2 (&v)[L], const float2* __restrict__ 
         const float2 t3 = rot<INV>(csub(v[1], v[3]));
         v[0] = cadd(t0, t2);
         v[2] = csub(t0, t2);
-        v[1] = cadd(t1, t3);
-        v[3] = csub(t1, t3);
+        // +-i (v1 - v3): a swapped pair, added lane by lane
+        v[1] = make_float2(t1.x + t3.x, t1.y + t3.y);
+        v[3] = make_float2(t1.x - t3.x, t1.y - t3.y);
     } else if constexpr (is_prime(C)) {
         // direct sums, pairing j and C - j: X_k = x0 + sum_j (x_j + x_{C-j}) cos
         //                                        -/+ i (x_j - x_{C-j}) sin

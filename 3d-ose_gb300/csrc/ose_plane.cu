@@ -16,11 +16,12 @@
 // 512 KiB plane changes hands between the two through distributed shared
 // memory: each CTA pushes the 32 x 32 blocks it holds into their owners'
 // receive buffers with st.async, whose bytes complete a transaction count on
-// the receiver's mbarrier, so a receiver waits on its own barrier and no
-// cluster-scope release (which would also wait for every global store in
-// flight, such as the epilogue's) is needed.  One relaxed cluster barrier per
-// exchange tells the senders that the receive buffers (which overlay the
-// transpose buffer) are free.
+// the receiver's mbarrier, so a receiver waits on its own barrier.  One
+// cluster barrier per exchange tells the senders that the receive buffers
+// (which overlay the transpose buffer) are free: a release arrive, so this
+// CTA's reads of the buffer are ordered before the other CTAs' pushes (a
+// relaxed arrive after a __syncthreads measured faster but let pushes overtake
+// reads still in flight).
 //
 // Every 256-point transform is a four-step 16 x 16 FFT: a line is held by 16
 // threads with 16 values each, a radix-16 DFT runs in registers, twiddles
@@ -60,11 +61,15 @@ constexpr int ECH_SUM = OSE_PLANE_ECH_SUM;   // the same where S is read and wri
 #endif
 constexpr int ECH_LAST = OSE_PLANE_ECH_LAST;  // the last application (S read, the state written)
 constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
+#ifndef OSE_PLANE_PUSH
+#define OSE_PLANE_PUSH 1
+#endif
+constexpr bool PUSH = OSE_PLANE_PUSH != 0;
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
-constexpr int TCOLS = 16 * 16 * SL;    // complex values in the column exchange buffer
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
+constexpr int MAIN = TROWS > ABUF ? TROWS : ABUF;   // transpose buffer = receive buffer
 // + twiddle table (hi, lo) + the x sponge factor's powers ax, ax^2, ax^3 (3 N floats)
-constexpr int SMEM_COMPLEX = (TROWS > ABUF ? TROWS : ABUF) + 2 * N + 3 * N / 2;
+constexpr int SMEM_COMPLEX = MAIN + 2 * N + 3 * N / 2;
 // + the exchange's mbarrier
 constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX + 16;
 
@@ -86,9 +91,49 @@ __device__ __forceinline__ float2 rot(float2 a)
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
+#ifndef OSE_PACKED
+#define OSE_PACKED 1
+#endif
+// Complex add and subtract as one packed two-lane FP32 instruction each
+// (add/sub.rn.f32x2: the same IEEE results as two scalar operations).
+__device__ __forceinline__ uint64_t pk2(float2 a)
+{
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(uint64_t r)
+{
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ float2 padd(float2 a, float2 b)
+{
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+__device__ __forceinline__ float2 psub(float2 a, float2 b)
+{
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+
 template <bool INV>
 __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3)
 {
+    if (OSE_PACKED) {
+        // the +-i (a1 - a3) terms stay scalar: a swapped pair is no packed operand
+        const float2 t0 = padd(a0, a2), t1 = psub(a0, a2), t2 = padd(a1, a3), d = psub(a1, a3);
+        a0 = padd(t0, t2);
+        a2 = psub(t0, t2);
+        const float2 t3 = rot<INV>(d);
+        a1 = make_float2(t1.x + t3.x, t1.y + t3.y);
+        a3 = make_float2(t1.x - t3.x, t1.y - t3.y);
+        return;
+    }
     const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = rot<INV>(csub(a1, a3));
     a0 = cadd(t0, t2);
     a2 = csub(t0, t2);
@@ -163,19 +208,15 @@ __device__ __forceinline__ void dft16(float2 (&v)[16])
     t = v[11]; v[11] = v[14]; v[14] = t;
 }
 
-#ifndef OSE_PLANE_PUSH
-#define OSE_PLANE_PUSH 1
-#endif
-constexpr bool PUSH = OSE_PLANE_PUSH != 0;
 // bytes each CTA receives per exchange: a 32 x 32 block from each other CTA
 constexpr unsigned PUSH_BYTES = (CL - 1) * SL * SL * sizeof(float2);
 constexpr uint64_t PUSH_WAIT_NS = 2000000000ull;   // then the error word is set
 constexpr int ERR_PLANE_EXCHANGE = 3;
 
-__device__ __forceinline__ void cluster_arrive_relaxed()
-{
-    asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
-}
+// Arrive with release semantics: this thread's earlier reads of its shared
+// memory (and the barrier initialisation) are ordered before the other CTAs'
+// pushes that follow their wait.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait;" ::: "memory"); }
 
 // The shared::cluster address of shared-memory address a in CTA `rank`.
@@ -322,8 +363,8 @@ __device__ __forceinline__ void exchange(float2* T, float2 (&v0)[16], float2 (&v
 // Four-step 256-point transform.  Forward: v[n1] = x[16 n1 + j] in,
 // v[k2] = X[j + 16 k2] out.  Inverse: the reverse.  LOCAL_IN: v0/v1 were
 // read from a receive buffer that T overlays, so all threads finish reading
-// before T is written.  ARRIVE: arrive (relaxed) at the cluster barrier once
-// this CTA's reads of T are done, so the other CTAs may push into it.
+// before T is written.  ARRIVE: arrive at the cluster barrier once this CTA's
+// reads of T are done, so the other CTAs may push into it.
 template <bool INV, bool ROWS, bool LOCAL_IN = false, bool ARRIVE = false>
 __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)[16], float2 (&v1)[16])
 {
@@ -337,7 +378,7 @@ __device__ __forceinline__ void fft256(float2* T, const float2* tw, float2 (&v0)
     }
     if (LOCAL_IN) __syncthreads();
     exchange<ROWS>(T, v0, v1);
-    if (ARRIVE) cluster_arrive_relaxed();
+    if (ARRIVE) cluster_arrive();
     dft16<INV>(v0);
     if (NS > 1) dft16<INV>(v1);
 }
@@ -640,7 +681,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     float2* T = smem;
     if (PUSH) {
         fft256<true, false, false, true>(T, tw, v0, v1);
-        cluster_wait();   // every CTA's transpose buffer is free
+        cluster_wait();   // every CTA's transpose buffer is free, its barrier initialised
         push_cols_to_rows(smem, xc, v0, v1, r);
         receive(xc, FWD);
         // rows 32r..: thread (row, j) takes kx = j + 16 k2
