@@ -83,8 +83,14 @@ template <int C>
 struct Cfg {
     static constexpr int L = 16 * C;
     static constexpr int P = C > 16 ? C : 16;      // line threads
-    static constexpr int TX = P > 16 ? 8 : 16;     // columns per CTA (y, z passes)
-    static constexpr int RW = P > 16 ? 8 : 16;     // rows per CTA (x passes)
+    // columns per CTA (y, z passes): 16 up to C = 20 (288 or 320 threads,
+    // two CTAs per SM; for C = 18 this measured 1.77 -> 1.55 ms per step of
+    // the padded 142^3 grid against 8 columns at three CTAs of 144 threads),
+    // 8 for C = 24 (16 would spill)
+    static constexpr int TX = P > 20 ? 8 : 16;
+    static constexpr bool CWIDE = TX * P > 256;    // launched two per SM: registers capped
+    // rows per CTA (x passes); 16 rows at C = 18 measured slower (spills)
+    static constexpr int RW = P > 16 ? 8 : 16;
     static constexpr int CTHREADS = TX * P;
     static constexpr int RTHREADS = RW * P;
     static constexpr int NP = 17 * C;              // padded row of the row transpose buffer
@@ -168,7 +174,7 @@ __device__ __forceinline__ void load_tables(float2* W, float2* B, float2* ch, co
 // y lines (AXIS 1) or z lines (AXIS 2) of TX columns; MODE as ose_cols.cu:
 // 0 forward, 1 inverse, 2 forward * |k| inverse.
 template <int C, int MODE>
-__global__ void __launch_bounds__(Cfg<C>::CTHREADS) k_col_bs(float2* __restrict__ X, int nxb, long long stride,
+__global__ void __launch_bounds__(Cfg<C>::CTHREADS, Cfg<C>::CWIDE ? 2 : 0) k_col_bs(float2* __restrict__ X, int nxb, long long stride,
                                                              long long ostride, int n, int axis, Tables tb)
 {
     using K = Cfg<C>;
@@ -261,7 +267,8 @@ __global__ void __launch_bounds__(Cfg<C>::RTHREADS) k_row_bs(const float2* __res
     }
 }
 
-#define OSE_BS_SIZES(X) X(4) X(8) X(12) X(18) X(20) X(24)
+// L = 16 C >= 2 n - 1 for 128 <= n <= 192: C from 16; 18, 20 and 24 cover it
+#define OSE_BS_SIZES(X) X(18) X(20) X(24)
 
 template <int C>
 cudaError_t configure_one()
@@ -338,7 +345,7 @@ int bluestein_length(int n)
     for (int f = 2; f <= t; ++f)
         while (t % f == 0) { t /= f; big = f; }
     if (big < 11) return 0;
-    static const int cs[] = {4, 8, 12, 18, 20, 24};
+    static const int cs[] = {18, 20, 24};
     for (int c : cs)
         if (16 * c >= 2 * n - 1) return 16 * c;
     return 0;
