@@ -28,6 +28,7 @@
 #include "ose_dft.cuh"
 #include "ose_epilogue.cuh"
 #include "ose_internal.h"
+#include "ose_pdl.cuh"
 
 namespace ose {
 namespace blue {
@@ -184,6 +185,8 @@ __global__ void __launch_bounds__(Cfg<C>::CTHREADS, Cfg<C>::CWIDE ? 2 : 0) k_col
     float2* ch = B + K::L;
     float2* T = ch + K::NMAX;
     load_tables(W, B, ch, tb.btw[axis], tb.bsp[axis], tb.bch[axis], K::L, n);
+    griddep_launch();   // launched with launch_pdl: only the constant tables are read before the wait
+    griddep_wait();
     const int c = threadIdx.x % K::TX, p = threadIdx.x / K::TX;
     const int x = blockIdx.x * K::TX + c, other = blockIdx.y;
     const bool ok = x < nxb && p < C;
@@ -236,6 +239,8 @@ __global__ void __launch_bounds__(Cfg<C>::RTHREADS) k_row_bs(const float2* __res
     float2* ch = B + K::L;
     float2* T = ch + K::NMAX;
     load_tables(W, B, ch, tb.btw[0], tb.bsp[0], tb.bch[0], K::L, n);
+    griddep_launch();
+    griddep_wait();
     const int r = threadIdx.x / K::P, q = threadIdx.x % K::P;
     const long long row = (long long)blockIdx.x * K::RW + r;
     const bool ok = row < nrows && q < C;
@@ -296,10 +301,9 @@ cudaError_t launch_col_c(cudaStream_t s, int mode, int n, float2* X, int nxb, in
 {
     using K = Cfg<C>;
     const dim3 grid((nxb + K::TX - 1) / K::TX, nother);
-    if (mode == 0) k_col_bs<C, 0><<<grid, K::CTHREADS, K::CSMEM, s>>>(X, nxb, stride, ostride, n, axis, t);
-    else if (mode == 1) k_col_bs<C, 1><<<grid, K::CTHREADS, K::CSMEM, s>>>(X, nxb, stride, ostride, n, axis, t);
-    else k_col_bs<C, 2><<<grid, K::CTHREADS, K::CSMEM, s>>>(X, nxb, stride, ostride, n, axis, t);
-    return cudaGetLastError();
+    if (mode == 0) return launch_pdl(k_col_bs<C, 0>, grid, dim3(K::CTHREADS), K::CSMEM, s, X, nxb, stride, ostride, n, axis, t);
+    if (mode == 1) return launch_pdl(k_col_bs<C, 1>, grid, dim3(K::CTHREADS), K::CSMEM, s, X, nxb, stride, ostride, n, axis, t);
+    return launch_pdl(k_col_bs<C, 2>, grid, dim3(K::CTHREADS), K::CSMEM, s, X, nxb, stride, ostride, n, axis, t);
 }
 
 template <int C>
@@ -307,26 +311,20 @@ cudaError_t launch_row_c(cudaStream_t s, int epi, int n, const float2* src, floa
                          const Tables& t, const EpiArgs& e)
 {
     using K = Cfg<C>;
-    const unsigned grid = (unsigned)((nrows + K::RW - 1) / K::RW);
+    const dim3 grid((unsigned)((nrows + K::RW - 1) / K::RW)), block(K::RTHREADS);
     switch (epi) {
     case EPI_NONE:
-        k_row_bs<C, EPI_NONE, false><<<grid, K::RTHREADS, K::RSMEM, s>>>(src, dst, n, nyb, nrows, t, e);
-        break;
+        return launch_pdl(k_row_bs<C, EPI_NONE, false>, grid, block, K::RSMEM, s, src, dst, n, nyb, nrows, t, e);
     case EPI_FIRST_FWD:
-        k_row_bs<C, EPI_FIRST, true><<<grid, K::RTHREADS, K::RSMEM, s>>>(src, dst, n, nyb, nrows, t, e);
-        break;
+        return launch_pdl(k_row_bs<C, EPI_FIRST, true>, grid, block, K::RSMEM, s, src, dst, n, nyb, nrows, t, e);
     case EPI_MID_FWD:
-        k_row_bs<C, EPI_MID, true><<<grid, K::RTHREADS, K::RSMEM, s>>>(src, dst, n, nyb, nrows, t, e);
-        break;
+        return launch_pdl(k_row_bs<C, EPI_MID, true>, grid, block, K::RSMEM, s, src, dst, n, nyb, nrows, t, e);
     case EPI_LAST:
-        k_row_bs<C, EPI_LAST, false><<<grid, K::RTHREADS, K::RSMEM, s>>>(src, dst, n, nyb, nrows, t, e);
-        break;
+        return launch_pdl(k_row_bs<C, EPI_LAST, false>, grid, block, K::RSMEM, s, src, dst, n, nyb, nrows, t, e);
     case EPI_SCALE:
-        k_row_bs<C, EPI_SCALE, false><<<grid, K::RTHREADS, K::RSMEM, s>>>(src, dst, n, nyb, nrows, t, e);
-        break;
+        return launch_pdl(k_row_bs<C, EPI_SCALE, false>, grid, block, K::RSMEM, s, src, dst, n, nyb, nrows, t, e);
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 }  // namespace blue
