@@ -92,6 +92,10 @@ struct Cfg {
     static constexpr bool CWIDE = TX * P > 256;    // launched two per SM: registers capped
     // rows per CTA (x passes); 16 rows at C = 18 measured slower (spills)
     static constexpr int RW = P > 16 ? 8 : 16;
+    // row CTAs per SM the registers must allow: 4 at C = 18 (96 registers, no
+    // spill; 1.52 -> 1.48 ms per step of the padded 142^3 grid against three
+    // CTAs at 125 registers); C = 20 and 24 would spill
+    static constexpr int RMINB = C == 18 ? 4 : 0;
     static constexpr int CTHREADS = TX * P;
     static constexpr int RTHREADS = RW * P;
     static constexpr int NP = 17 * C;              // padded row of the row transpose buffer
@@ -229,7 +233,7 @@ __global__ void __launch_bounds__(Cfg<C>::CTHREADS, Cfg<C>::CWIDE ? 2 : 0) k_col
 // transform of src into dst.  Otherwise the inverse transform of src, the
 // step's epilogue and (FWD) the forward transform of the new term into dst.
 template <int C, int EPI, bool FWD>
-__global__ void __launch_bounds__(Cfg<C>::RTHREADS) k_row_bs(const float2* __restrict__ src, float2* __restrict__ dst,
+__global__ void __launch_bounds__(Cfg<C>::RTHREADS, Cfg<C>::RMINB) k_row_bs(const float2* __restrict__ src, float2* __restrict__ dst,
                                                              int n, int nyb, long long nrows, Tables tb, EpiArgs e)
 {
     using K = Cfg<C>;

@@ -165,6 +165,11 @@ struct RowCfg {
     static constexpr int THREADS = RW * P;
     static constexpr int NP = 17 * C;              // padded row of the transpose buffer
     static constexpr size_t SMEM = sizeof(float2) * ((size_t)N + (size_t)RW * NP);
+    // CTAs per SM asked of the register allocator: 4 where a CTA has at most
+    // 160 threads (C = 18, 20: 96 registers, a few spilled in the epilogue
+    // instances; 320 x 288 x 256 measured 4.41 -> 4.36 ms per step against
+    // three CTAs at 111-115 registers); none otherwise
+    static constexpr int MINB = THREADS <= 160 ? 4 : 0;
 };
 
 // x rows (contiguous, row = z * nyb + y) of row block rb.  EPI_NONE: forward
@@ -252,7 +257,7 @@ __device__ __forceinline__ void row_body(const float2* __restrict__ src, float2*
 }
 
 template <int C, int EPI, bool FWD = false>
-__global__ void __launch_bounds__(RowCfg<C>::THREADS) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
+__global__ void __launch_bounds__(RowCfg<C>::THREADS, RowCfg<C>::MINB) k_row(const float2* __restrict__ src, float2* __restrict__ dst,
                                                             int nyb, long long nrows, const float2* __restrict__ twg,
                                                             EpiArgs e)
 {

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include "ose_internal.h"
+#include "ose_pdl.cuh"
 #include "ose_epilogue.cuh"
 
 namespace ose {
@@ -488,6 +489,10 @@ cudaError_t launch_apply_operator(cudaStream_t s, const Geometry& g, const AxisP
 // so a captured graph can replay it.
 __global__ void k_inject(float2* W, long long src, const float* ricker, const float* hil, int* ctr, int nt)
 {
+    // launched with launch_pdl: the step's first transform may start its
+    // table loads meanwhile; everything here comes after the wait
+    griddep_launch();
+    griddep_wait();
     const int it = ctr[0];
     ctr[1] = it;
     ctr[0] = it + 1;
@@ -502,8 +507,7 @@ __global__ void k_inject(float2* W, long long src, const float* ricker, const fl
 cudaError_t launch_inject(cudaStream_t s, float2* W, long long src, const float* ricker,
                           const float* hil, int* ctr, int nt)
 {
-    k_inject<<<1, 1, 0, s>>>(W, src, ricker, hil, ctr, nt);
-    return cudaGetLastError();
+    return launch_pdl(k_inject, dim3(1), dim3(1), 0, s, W, src, ricker, hil, ctr, nt);
 }
 
 /* ---- batched shots ---------------------------------------------------------

@@ -1,5 +1,7 @@
 // ose_pdl.cuh - programmatic dependent launch for the plane-path kernels
-// (ose_plane.cu; the generic path's passes measured slower with it).
+// (ose_plane.cu), the Bluestein passes (ose_bluestein.cu) and the source
+// injection; the generic path's register and Stockham passes measured slower
+// with it and launch plainly.
 //
 // A kernel launched with launch_pdl may start its CTAs while the kernel
 // before it in the stream still runs its last wave; griddep_wait() blocks
