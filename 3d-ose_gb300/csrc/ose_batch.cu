@@ -581,7 +581,7 @@ static ose_status persist_status(ose_batch* b)
     BCK(b, cudaMemcpy(&w, b->d_bar + 2, sizeof w, cudaMemcpyDeviceToHost));
     if (w) {
         cudaMemset(b->d_bar + 2, 0, sizeof w);
-        return bfail(b, OSE_ERR_CUDA, "persistent batched step: a grid barrier timed out");
+        return bfail(b, OSE_ERR_TIMEOUT, "persistent batched step: a grid barrier timed out");
     }
     return OSE_OK;
 }

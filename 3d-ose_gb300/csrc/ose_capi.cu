@@ -341,7 +341,7 @@ ose_status tensor_status(ose_handle* h)
     CK(h, cudaMemcpy(&v, h->tcerr, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
         CK(h, cudaMemset(h->tcerr, 0, sizeof(int)));
-        return fail(h, OSE_ERR_CUDA, v == 3   ? "plane kernels: a DSMEM exchange wait ran out of time"
+        return fail(h, OSE_ERR_TIMEOUT, v == 3 ? "plane kernels: a DSMEM exchange wait ran out of time"
                                      : v == 2 ? "boundary corrector: an MMA completion wait ran out of time"
                                               : "tensor-core z pass: an MMA completion wait ran out of time");
     }
@@ -447,6 +447,30 @@ ose_status ose_padded_dims(const ose_params* p, int* nxb, int* nyb, int* nzb)
 }
 
 const char* ose_last_error(const ose_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+ose_status ose_self_test_waits(double limit_ms, int* expired)
+{
+    if (!expired || !(limit_ms > 0.0 && limit_ms <= 100.0))
+        return fail(nullptr, OSE_ERR_INVALID, "ose_self_test_waits: limit_ms must be in (0, 100]");
+    *expired = 0;
+    int* d = nullptr;   // error words [0..2], grid barrier words [4..5]
+    cudaStream_t s = nullptr;
+    const unsigned long long ns = (unsigned long long)(limit_ms * 1e6);
+    int w[3] = {0, 0, 0};
+    cudaError_t e = cudaMalloc((void**)&d, 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 8 * sizeof(int), s);
+    if (e == cudaSuccess) e = ose::selftest_exchange_wait(s, d + 0, ns);
+    if (e == cudaSuccess) e = ose::selftest_grid_barrier(s, reinterpret_cast<unsigned*>(d + 4), d + 1, ns);
+    if (e == cudaSuccess) e = ose::selftest_mma_wait(s, d + 2, ns);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(w, d, sizeof w, cudaMemcpyDeviceToHost);
+    if (s) cudaStreamDestroy(s);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return fail(nullptr, OSE_ERR_CUDA, std::string("ose_self_test_waits: ") + cudaGetErrorString(e));
+    *expired = (w[0] ? 1 : 0) | (w[1] ? 2 : 0) | (w[2] ? 4 : 0);
+    return OSE_OK;
+}
 
 ose_status ose_get_derived(const ose_handle* h, ose_derived* d)
 {

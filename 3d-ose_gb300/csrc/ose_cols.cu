@@ -314,22 +314,25 @@ __device__ __forceinline__ unsigned long long now_ns()
 }
 
 // bar[0] = arrivals, bar[1] = generation.  Returns false after a timeout.
-__device__ bool grid_barrier(unsigned* bar, int* err)
+// expected = the CTAs that arrive (the grid; the self test asks for more).
+__device__ bool grid_barrier(unsigned* bar, int* err, unsigned long long limit_ns = kBarrierLimitNs,
+                             unsigned expected = 0)
 {
+    if (expected == 0) expected = gridDim.x;
     __syncthreads();
     int ok = 1;
     if (threadIdx.x == 0) {
         volatile unsigned* gen = bar + 1;
         const unsigned g = *gen;
         __threadfence();
-        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+        if (atomicAdd(bar, 1u) + 1u == expected) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
             const unsigned long long t0 = now_ns();
             while (*gen == g) {
-                if (now_ns() - t0 > kBarrierLimitNs) {
+                if (now_ns() - t0 > limit_ns) {
                     ok = 0;
                     atomicExch(err, 1);
                     break;
@@ -342,6 +345,13 @@ __device__ bool grid_barrier(unsigned* bar, int* err)
     const bool all = __syncthreads_and(ok) != 0;
     __threadfence();   // every thread orders its later loads after the barrier
     return all;
+}
+
+// Self test of the bounded grid barrier: one CTA waits for a second one that
+// is never launched, so the wait runs out after limit_ns and sets *err.
+__global__ void k_selftest_grid_barrier(unsigned* bar, int* err, unsigned long long limit_ns)
+{
+    grid_barrier(bar, err, limit_ns, gridDim.x + 1);
 }
 
 template <int C>
@@ -562,6 +572,12 @@ cudaError_t launch_col(cudaStream_t s, int mode, int n, float2* X, int nxb, int 
 #undef LAUNCH
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t selftest_grid_barrier(cudaStream_t s, unsigned* bar, int* err, unsigned long long limit_ns)
+{
+    cols::k_selftest_grid_barrier<<<1, 32, 0, s>>>(bar, err, limit_ns);
+    return cudaGetLastError();
 }
 
 }  // namespace ose

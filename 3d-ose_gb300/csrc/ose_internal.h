@@ -252,6 +252,14 @@ cudaError_t launch_plane_apply_operator(cudaStream_t s, const float2* in, float2
                                         const float* vs, float sch, float scl, const Tables& t);
 int plane_max_active_clusters();
 
+// Self tests of the bounded waits (one CTA each; nothing ever completes the
+// wait, so it runs out after limit_ns and the kernel sets *err, non-zero):
+// the plane kernels' DSMEM exchange wait, the persistent batch's grid barrier
+// (bar: two zeroed words) and the tensor-core MMA completion wait.
+cudaError_t selftest_exchange_wait(cudaStream_t s, int* err, unsigned long long limit_ns);
+cudaError_t selftest_grid_barrier(cudaStream_t s, unsigned* bar, int* err, unsigned long long limit_ns);
+cudaError_t selftest_mma_wait(cudaStream_t s, int* err, unsigned long long limit_ns);
+
 // Axis transforms by Bluestein's chirp-z identity (ose_bluestein.cu).
 int bluestein_length(int n);
 void bluestein_tables(int n, int L, std::vector<float2>& chirp, std::vector<float2>& spec,

@@ -304,6 +304,20 @@ __device__ __forceinline__ void receive(Exchange& x, bool more)
     __syncthreads();
 }
 
+// Self test of the bounded exchange wait: the barrier is armed for an
+// exchange that no CTA ever pushes, so every thread's wait runs out after
+// limit_ns and the error word is set.
+__global__ void k_selftest_exchange_wait(int* err, unsigned long long limit_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc5::mbar_init(&bar, 1);
+        arm(&bar);
+    }
+    __syncthreads();
+    if (!wait_pushed(&bar, 0u, limit_ns)) atomicExch(err, ERR_PLANE_EXCHANGE);
+}
+
 // Rows context (x transforms): slot s of thread t handles row
 // (warp + WARPS s) * 2 + lane / 16 and line thread j = lane % 16.
 struct RowSlot {
@@ -871,6 +885,12 @@ cudaError_t launch_zpass(cudaStream_t s, float2* X, const Tables& t)
     return launch_pdl(plane::k_zpass16<false>, dim3(plane::N / plane::ZW, plane::N), dim3(plane::ZTHREADS),
                       plane::ZSMEM_BYTES, s, X, (const float2*)t.twx, t, (int)plane::N,
                       (long long)plane::N * plane::N);
+}
+
+cudaError_t selftest_exchange_wait(cudaStream_t s, int* err, unsigned long long limit_ns)
+{
+    plane::k_selftest_exchange_wait<<<1, 64, 0, s>>>(err, limit_ns);
+    return cudaGetLastError();
 }
 
 bool zpass256_supported(const Geometry& g) { return g.nzb == plane::N && g.nxb % plane::ZW == 0; }

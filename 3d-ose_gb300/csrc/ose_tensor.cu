@@ -338,4 +338,20 @@ cudaError_t launch_tensor_zpass(cudaStream_t s, float2* X, const Geometry& g, co
     }
 }
 
+// Self test of the bounded MMA-completion wait (tc5::mbar_wait, as the
+// tensor z pass and the corrector use it): a barrier no commit ever reaches.
+__global__ void k_selftest_mma_wait(int* err, unsigned long long limit_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) tc5::mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && !tc5::mbar_wait(&bar, 0u, limit_ns)) atomicExch(err, 1);
+}
+
+cudaError_t selftest_mma_wait(cudaStream_t s, int* err, unsigned long long limit_ns)
+{
+    k_selftest_mma_wait<<<1, 32, 0, s>>>(err, limit_ns);
+    return cudaGetLastError();
+}
+
 }  // namespace ose

@@ -27,11 +27,12 @@ PRECISIONS = {"fp32": PRECISION_FP32, "tf32": PRECISION_TF32, "tf32x3": PRECISIO
 NOALLOC_MAX_CELLS = 262144   # OSE_NOALLOC_MAX_CELLS
 
 STATUS = {0: "OSE_OK", 1: "OSE_ERR_INVALID", 2: "OSE_ERR_CUDA", 3: "OSE_ERR_NOMEM",
-          4: "OSE_ERR_IO", 5: "OSE_ERR_UNSUPPORTED", 6: "OSE_ERR_STATE", 7: "OSE_ERR_NUMERIC"}
+          4: "OSE_ERR_IO", 5: "OSE_ERR_UNSUPPORTED", 6: "OSE_ERR_STATE", 7: "OSE_ERR_NUMERIC",
+          8: "OSE_ERR_TIMEOUT"}
 
 # Every symbol include/ose3d.h declares.
 EXPORTS = ["ose_default_params", "ose_padded_dims", "ose_create", "ose_create_from_file",
-           "ose_destroy", "ose_last_error", "ose_get_derived", "ose_reset_shot", "ose_step",
+           "ose_destroy", "ose_last_error", "ose_get_derived", "ose_self_test_waits", "ose_reset_shot", "ose_step",
            "ose_run", "ose_run_record", "ose_run_timed", "ose_select_path", "ose_get_it", "ose_get_wavefield", "ose_set_wavefield",
            "ose_get_gather", "ose_get_wavelets", "ose_get_sponge", "ose_apply_operator",
            "ose_profile_step", "ose_write_outputs", "ose_version", "ose_apply_operator_noalloc",
@@ -115,6 +116,7 @@ def load_library(path: str = LIB_PATH):
         "ose_destroy": ([H], ctypes.c_int),
         "ose_last_error": ([H], ctypes.c_char_p),
         "ose_get_derived": ([H, P(Derived)], ctypes.c_int),
+        "ose_self_test_waits": ([ctypes.c_double, P(ctypes.c_int)], ctypes.c_int),
         "ose_reset_shot": ([H, ctypes.c_int], ctypes.c_int),
         "ose_step": ([H], ctypes.c_int),
         "ose_run": ([H, ctypes.c_int, f32], ctypes.c_int),
@@ -192,6 +194,19 @@ def apply_operator_noalloc(nxb: int, nyb: int, nzb: int, dx: float, dy: float, d
     return load_library().ose_apply_operator_noalloc(
         nxb, nyb, nzb, dx, dy, dz, R, ctypes.c_void_p(vel_ptr), ctypes.c_void_p(in_ptr),
         ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream) if stream else None)
+
+
+def self_test_waits(limit_ms: float = 5.0) -> int:
+    """ose_self_test_waits: run each bounded in-kernel wait (plane exchange,
+    persistent-batch grid barrier, MMA completion) against something that
+    never completes, with limit_ms instead of the production limit; returns
+    the mask of waits that ran out and recorded it (7 = all three)."""
+    L = load_library()
+    out = ctypes.c_int(0)
+    st = L.ose_self_test_waits(float(limit_ms), ctypes.byref(out))
+    if st != 0:
+        raise OseError(st, L.ose_last_error(None).decode())
+    return out.value
 
 
 def default_params(**kw) -> Params:

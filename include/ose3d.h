@@ -37,7 +37,11 @@ typedef enum ose_status {
     OSE_ERR_IO = 4,           /* file could not be read or written */
     OSE_ERR_UNSUPPORTED = 5,  /* size or mode outside what the kernels handle */
     OSE_ERR_STATE = 6,        /* call out of order (e.g. ose_step before ose_reset_shot) */
-    OSE_ERR_NUMERIC = 7       /* non-finite value found in the wavefield */
+    OSE_ERR_NUMERIC = 7,      /* non-finite value found in the wavefield */
+    OSE_ERR_TIMEOUT = 8       /* a bounded wait inside a kernel ran out of time (2 s for the
+                                 plane exchange and the batch's grid barrier, 1 s for an MMA
+                                 completion); the results of that call are invalid, the
+                                 device context stays usable */
 } ose_status;
 
 /* Sponge profile.  REFERENCE is generate_att (ose_3d_kernel.cu:242-261):
@@ -130,6 +134,17 @@ ose_status ose_destroy(ose_handle* h);
 const char* ose_last_error(const ose_handle* h);
 
 ose_status ose_get_derived(const ose_handle* h, ose_derived* d);
+
+/* Self test of the bounded waits inside the kernels (no counterpart in the
+ * reference, which has none): one single-CTA kernel per kind waits on
+ * something that never completes — the plane kernels' DSMEM exchange
+ * mbarrier, the persistent batch's grid barrier, the tensor-core MMA
+ * completion barrier — with a limit of limit_ms (0 < limit_ms <= 100) instead
+ * of the production 1-2 s.  *expired gets bit 0, 1, 2 set for each wait that
+ * ran out and recorded it in its error word (7 = all three behave); the
+ * device context stays usable.  Runs on its own stream; no handle needed
+ * (ose_last_error(NULL) on failure). */
+ose_status ose_self_test_waits(double limit_ms, int* expired);
 
 /* Start shot `is`: zero P and Q, rebuild the shot's Ricker and Hilbert traces,
  * clear the device gather and set it = 0.  Replaces Xtdata_value +
@@ -377,7 +392,7 @@ ose_status ose_batch_get_wavefield(ose_batch* b, int shot, int which, float* out
  * lanes = -1: the source injection and then ONE persistent cooperative
  * launch per step that runs every batched pass, with grid barriers between
  * passes — available when every axis length is 16 C with C <= 16; a barrier
- * that waits longer than 2 s ends the step with OSE_ERR_CUDA),
+ * that waits longer than 2 s ends the step with OSE_ERR_TIMEOUT),
  * the shot grouping of batched launches (groups whose working set stays
  * within group_mb MB, so a group's fields can stay in L2 through its step;
  * 0 = all shots together) and, for axis lengths without register kernels, the rows

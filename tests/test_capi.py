@@ -67,6 +67,21 @@ def test_null_handle_calls_are_errors(lib):
     assert lib.ose_version().startswith(b"ose3d")
 
 
+def test_status_codes_mirror_the_header():
+    import re
+    src = open(os.path.join(ROOT, "include", "ose3d.h")).read()
+    codes = {int(v): k for k, v in re.findall(r"\b(OSE_(?:OK|ERR_[A-Z]+))\s*=\s*(\d+)", src)}
+    assert codes == ose3d.STATUS
+
+
+def test_wait_self_test_rejects_bad_limits_before_the_device(lib):
+    out = ctypes.c_int(-1)
+    for bad in (0.0, -1.0, 1000.0, float("nan")):
+        assert lib.ose_self_test_waits(bad, ctypes.byref(out)) == 1
+    assert lib.ose_self_test_waits(5.0, None) == 1
+    assert b"limit_ms" in lib.ose_last_error(None)
+
+
 def test_python_class_mirrors_header_structs():
     assert ctypes.sizeof(ose3d.Params) == ctypes.sizeof(O.OseParams)
     assert [f[0] for f in ose3d.Params._fields_] == [f[0] for f in O.OseParams._fields_]
