@@ -25,36 +25,28 @@ __host__ __device__ constexpr int first_factor(int n)
     return n;
 }
 
-#ifndef OSE_PACKED
-#define OSE_PACKED 1
-#endif
-// With OSE_PACKED a complex add or subtract is one packed two-lane FP32
-// instruction (add/sub.rn.f32x2: the same IEEE results as two scalar ones).
+// A complex add or subtract is one packed two-lane FP32 instruction
+// (add/sub.rn.f32x2: the same IEEE results as two scalar ones, never
+// contracted with a preceding multiply).
 __device__ __forceinline__ float2 cadd(float2 a, float2 b)
 {
-    if (OSE_PACKED) {
-        unsigned long long d, x, y;
-        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
-        asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
-        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
-        float2 r;
-        asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
-        return r;
-    }
-    return make_float2(a.x + b.x, a.y + b.y);
+    unsigned long long d, x, y;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+    return r;
 }
 __device__ __forceinline__ float2 csub(float2 a, float2 b)
 {
-    if (OSE_PACKED) {
-        unsigned long long d, x, y;
-        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
-        asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
-        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
-        float2 r;
-        asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
-        return r;
-    }
-    return make_float2(a.x - b.x, a.y - b.y);
+    unsigned long long d, x, y;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b.x), "f"(b.y));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x), "l"(y));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+    return r;
 }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {

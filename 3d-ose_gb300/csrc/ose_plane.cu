@@ -61,10 +61,6 @@ constexpr int ECH_SUM = OSE_PLANE_ECH_SUM;   // the same where S is read and wri
 #endif
 constexpr int ECH_LAST = OSE_PLANE_ECH_LAST;  // the last application (S read, the state written)
 constexpr int TPAD = 17;        // padded stride of the row-transpose buffer
-#ifndef OSE_PLANE_PUSH
-#define OSE_PLANE_PUSH 1
-#endif
-constexpr bool PUSH = OSE_PLANE_PUSH != 0;
 constexpr int TROWS = SL * 16 * TPAD;  // complex values in the row exchange buffer
 constexpr int ABUF = SL * N;           // complex values of one CTA's plane slice
 constexpr int MAIN = TROWS > ABUF ? TROWS : ABUF;   // transpose buffer = receive buffer
@@ -73,17 +69,6 @@ constexpr int SMEM_COMPLEX = MAIN + 2 * N + 3 * N / 2;
 // + the exchange's mbarrier
 constexpr size_t SMEM_BYTES = sizeof(float2) * SMEM_COMPLEX + 16;
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
-{
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-__device__ __forceinline__ float2 cmulc(float2 a, float2 b)   // a * conj(b)
-{
-    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
-}
-
 // times -i (forward) or +i (inverse)
 template <bool INV>
 __device__ __forceinline__ float2 rot(float2 a)
@@ -91,9 +76,6 @@ __device__ __forceinline__ float2 rot(float2 a)
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-#ifndef OSE_PACKED
-#define OSE_PACKED 1
-#endif
 // Complex add and subtract as one packed two-lane FP32 instruction each
 // (add/sub.rn.f32x2: the same IEEE results as two scalar operations).
 __device__ __forceinline__ uint64_t pk2(float2 a)
@@ -124,21 +106,13 @@ __device__ __forceinline__ float2 psub(float2 a, float2 b)
 template <bool INV>
 __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3)
 {
-    if (OSE_PACKED) {
-        // the +-i (a1 - a3) terms stay scalar: a swapped pair is no packed operand
-        const float2 t0 = padd(a0, a2), t1 = psub(a0, a2), t2 = padd(a1, a3), d = psub(a1, a3);
-        a0 = padd(t0, t2);
-        a2 = psub(t0, t2);
-        const float2 t3 = rot<INV>(d);
-        a1 = make_float2(t1.x + t3.x, t1.y + t3.y);
-        a3 = make_float2(t1.x - t3.x, t1.y - t3.y);
-        return;
-    }
-    const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = rot<INV>(csub(a1, a3));
-    a0 = cadd(t0, t2);
-    a2 = csub(t0, t2);
-    a1 = cadd(t1, t3);
-    a3 = csub(t1, t3);
+    // the +-i (a1 - a3) terms stay scalar: a swapped pair is no packed operand
+    const float2 t0 = padd(a0, a2), t1 = psub(a0, a2), t2 = padd(a1, a3), d = psub(a1, a3);
+    a0 = padd(t0, t2);
+    a2 = psub(t0, t2);
+    const float2 t3 = rot<INV>(d);
+    a1 = make_float2(t1.x + t3.x, t1.y + t3.y);
+    a3 = make_float2(t1.x - t3.x, t1.y - t3.y);
 }
 
 // times W_16^E (forward) or its conjugate (inverse); E in {0,1,2,3,4,6,9}.
@@ -282,7 +256,7 @@ __device__ __forceinline__ void arm(uint64_t* bar)
 __device__ __forceinline__ Exchange exchange_init(float2* smem, int* err)
 {
     Exchange x{reinterpret_cast<uint64_t*>(smem + SMEM_COMPLEX), err, 0u, true};
-    if (PUSH && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
         tc5::mbar_init(x.bar, 1);
         arm(x.bar);
     }
@@ -468,50 +442,23 @@ __device__ __forceinline__ void push_rows_to_cols(float2* R, const Exchange& xc,
 
 // Forward x FFT of this CTA's 32 rows (values in v0/v1, spatial order) then
 // forward y FFT of its 32 columns; spectrum stored to dst plane z.
-__device__ __forceinline__ void forward_xy(cg::cluster_group& cluster, float2* smem, const float2* tw,
+__device__ __forceinline__ void forward_xy(float2* smem, const float2* tw,
                                            float2 (&v0)[16], float2 (&v1)[16], float2* dst, int z, int r,
                                            Exchange& xc)
 {
     float2* T = smem;
-    if (PUSH) {
-        fft256<false, true, false, true>(T, tw, v0, v1);
-        cluster_wait();   // every CTA's transpose buffer is free
-        push_rows_to_cols(smem, xc, v0, v1, r);
-        receive(xc, false);
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const ColSlot q = col_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-            for (int n1 = 0; n1 < 16; ++n1) v[n1] = smem[(16 * n1 + q.j) * SL + q.c];
-        }
-        fft256<false, false, true>(T, tw, v0, v1);
-    } else {
-    fft256<false, true>(T, tw, v0, v1);
-    // natural-order rows into this CTA's slice A[row][kx]
-    float2* A = smem;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const RowSlot q = row_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2) A[q.row * N + q.j + 16 * k2] = v[k2];
-    }
-    cluster.sync();
-    // columns 32r..32r+31 of all 256 rows from the 8 slices
+    fft256<false, true, false, true>(T, tw, v0, v1);
+    cluster_wait();   // every CTA's transpose buffer is free
+    push_rows_to_cols(smem, xc, v0, v1, r);
+    receive(xc, false);
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         const ColSlot q = col_slot(s);
         float2(&v)[16] = s ? v1 : v0;
 #pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) {
-            const float2* rem = cluster.map_shared_rank(A, n1 >> 1);
-            v[n1] = rem[((16 * n1 + q.j) & (SL - 1)) * N + SL * r + q.c];
-        }
+        for (int n1 = 0; n1 < 16; ++n1) v[n1] = smem[(16 * n1 + q.j) * SL + q.c];
     }
-    cluster.sync();
-    fft256<false, false>(T, tw, v0, v1);
-    }
+    fft256<false, false, true>(T, tw, v0, v1);
     float2* out = dst + (size_t)z * N * N + SL * r;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -544,7 +491,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
         for (int n1 = 0; n1 < 16; ++n1) v[n1] = in[(size_t)q.row * N + 16 * n1 + q.j];
     }
     __syncthreads();
-    forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r, xc);
+    forward_xy(smem, tw, v0, v1, a.dst, z, r, xc);
 }
 
 // The pointwise update of one row slot (x = 16 n1 + j): scal_vr_3d, the
@@ -693,51 +640,23 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS, 2) k_plane
     }
     __syncthreads();
     float2* T = smem;
-    if (PUSH) {
-        fft256<true, false, false, true>(T, tw, v0, v1);
-        cluster_wait();   // every CTA's transpose buffer is free, its barrier initialised
-        push_cols_to_rows(smem, xc, v0, v1, r);
-        receive(xc, FWD);
-        // rows 32r..: thread (row, j) takes kx = j + 16 k2
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const RowSlot q = row_slot(s);
-            float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-            for (int k2 = 0; k2 < 16; ++k2) v[k2] = smem[q.row * N + q.j + 16 * k2];
-        }
-        fft256<true, true, true>(T, tw, v0, v1);
-    } else {
-    fft256<true, false>(T, tw, v0, v1);
-    // columns into this CTA's slice A[y][c]
-    float2* A = smem;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const ColSlot q = col_slot(s);
-        float2(&v)[16] = s ? v1 : v0;
-#pragma unroll
-        for (int n1 = 0; n1 < 16; ++n1) A[(16 * n1 + q.j) * SL + q.c] = v[n1];
-    }
-    cluster.sync();
-    // rows 32r..: thread (row, j) takes kx = j + 16 k2 from slice k2/2
+    fft256<true, false, false, true>(T, tw, v0, v1);
+    cluster_wait();   // every CTA's transpose buffer is free, its barrier initialised
+    push_cols_to_rows(smem, xc, v0, v1, r);
+    receive(xc, FWD);
+    // rows 32r..: thread (row, j) takes kx = j + 16 k2
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         const RowSlot q = row_slot(s);
         float2(&v)[16] = s ? v1 : v0;
-        const int y = SL * r + q.row;
 #pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2) {
-            const float2* rem = cluster.map_shared_rank(A, k2 >> 1);
-            v[k2] = rem[y * SL + q.j + 16 * (k2 & 1)];
-        }
+        for (int k2 = 0; k2 < 16; ++k2) v[k2] = smem[q.row * N + q.j + 16 * k2];
     }
-    cluster.sync();
-    fft256<true, true>(T, tw, v0, v1);
-    }
+    fft256<true, true, true>(T, tw, v0, v1);
     // pointwise update on (x = 16 n1 + j, y, z)
     epilogue_slot<EPI, SUM>(v0, a.e, axp, SL * r + row_slot(0).row, z, row_slot(0).j);
     if (NS > 1) epilogue_slot<EPI, SUM>(v1, a.e, axp, SL * r + row_slot(1).row, z, row_slot(1).j);
-    if (FWD) forward_xy(cluster, smem, tw, v0, v1, a.dst, z, r, xc);
+    if (FWD) forward_xy(smem, tw, v0, v1, a.dst, z, r, xc);
 }
 
 // z lines of a 16-wide kx tile at one ky: forward, * |k|, inverse, in place.
