@@ -329,8 +329,6 @@ ose_status build_graph(ose_handle* h)
     return OSE_OK;
 }
 
-ose_status check_handle(const ose_handle* h) { return h ? OSE_OK : OSE_ERR_INVALID; }
-
 // After the stream is idle: kernels with bounded waits (tensor-core z pass,
 // corrector, the plane kernels' exchanges) record a wait that ran out of time
 // in the handle's error word.
