@@ -51,6 +51,11 @@ struct ose_handle {
     std::vector<int> rec_xyz;
     int* ctr = nullptr;      // [0] next step, [1] current step
     size_t bytes = 0;
+    // fault injection for tests: the fail_alloc_at-th device allocation of
+    // ose_create fails as if the device were out of memory (0 = never; from
+    // OSE3D_FAIL_DEVICE_ALLOC in the environment)
+    int fail_alloc_at = 0;
+    int nalloc = 0;
     // precision form: mode, DFT operands of the tensor-core z pass, error word
     int precision = OSE_PRECISION_FP32;
     void* tcb = nullptr;
@@ -113,6 +118,7 @@ template <typename T>
 cudaError_t dalloc(ose_handle* h, T** p, size_t count)
 {
     size_t b = sizeof(T) * count;
+    if (h->fail_alloc_at > 0 && ++h->nalloc == h->fail_alloc_at) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc((void**)p, b);
     if (e == cudaSuccess) h->bytes += b;
     return e;
@@ -484,6 +490,7 @@ ose_status ose_create(const ose_params* pin, const float* vel, ose_handle** out)
     *out = nullptr;
     ose_handle* h = new (std::nothrow) ose_handle();
     if (!h) return fail(nullptr, OSE_ERR_NOMEM, "host allocation failed");
+    if (const char* fa = getenv("OSE3D_FAIL_DEVICE_ALLOC")) h->fail_alloc_at = atoi(fa);
     h->p = *pin;
     std::string err;
     if (ose::derive_dims(h->p, &h->d, &err)) { delete h; return fail(nullptr, OSE_ERR_INVALID, err); }

@@ -120,3 +120,17 @@ def test_create_rejects_before_touching_the_device(lib, case):
               "zero_velocity": (1, b"positive"), "nan_velocity": (1, b"finite")}[case]
     assert st == expect[0]
     assert expect[1] in lib.ose_last_error(None)
+
+
+def test_model_file_errors_before_the_device(lib, tmp_path):
+    p = ose3d.default_params(nx=8, ny=8, nz=8, bu=4, bd=4, bl=4, br=4, bf=4, bb=4, nt=4, sxbeg=4, sybeg=4,
+                             szbeg=2, gzbeg=0)
+    h = ctypes.c_void_p()
+    missing = str(tmp_path / "nothing.bin").encode()
+    assert lib.ose_create_from_file(ctypes.byref(p), missing, ctypes.byref(h)) == 4
+    assert b"cannot open" in lib.ose_last_error(None)
+    short = tmp_path / "short.bin"
+    np.full(8 * 8 * 8 - 1, 2000.0, np.float32).tofile(short)
+    assert lib.ose_create_from_file(ctypes.byref(p), str(short).encode(), ctypes.byref(h)) == 4
+    assert b"short model file" in lib.ose_last_error(None)
+    assert not h.value
